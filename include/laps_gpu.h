@@ -1,0 +1,176 @@
+/*
+ * laps_gpu.h - C-ABI of the GB300 engine for LAPS's right-hand-side evaluation and RK3
+ * time advance.
+ *
+ * The reference has no library interface: its hot path is a set of argument-less Fortran
+ * subroutines sharing module globals, called from the main program `mhd`
+ * (src_compressible/mhd.f90).  Each entry point below states which of those subroutines
+ * (file:line inside the reference project) it replaces.  A Fortran host binds them through
+ * `iso_c_binding` (see fortran/laps_gpu.f90); C, C++ and Python (ctypes) hosts bind them
+ * directly.
+ *
+ * Conventions
+ *  - All device memory is owned by the context.  Host arrays are owned by the caller and
+ *    are only read or written during the call.
+ *  - Real-space arrays use the reference's layout uu(ix,iy,iz,ivar): x fastest, then y,
+ *    then z, then the variable (Fortran column-major), float64.
+ *  - Every function returns 0 (LAPS_OK) or a negative LAPS_E* code; the text of the last
+ *    error is available from laps_last_error().  No C++ exception crosses this boundary.
+ *  - One host thread per context.  Each context owns one CUDA stream; calls are
+ *    asynchronous on it except where a host array or a scalar result is returned.
+ *  - Waits on the device are bounded: a wait that does not finish within the context's
+ *    timeout returns LAPS_ETIMEDOUT instead of blocking forever.
+ */
+#ifndef LAPS_GPU_H
+#define LAPS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- codes */
+#define LAPS_OK 0
+#define LAPS_EINVAL (-1)      /* bad argument or unsupported parameter combination */
+#define LAPS_ENOMEM (-2)      /* device allocation failed or above the configured cap */
+#define LAPS_ECUDA (-3)       /* CUDA runtime error */
+#define LAPS_ETIMEDOUT (-4)   /* a bounded wait on the device expired */
+#define LAPS_ESTATE (-5)      /* call out of order (e.g. step before upload) */
+
+/* status bits returned by laps_step / laps_vardt */
+#define LAPS_STATUS_NAN 1       /* a NaN was met in the CFL reduction */
+#define LAPS_STATUS_DT_FLOOR 2  /* dt < 1e-8: step not taken (src_compressible/mhd.f90:216) */
+
+/* variants (the reference ships one source tree per variant) */
+#define LAPS_VARIANT_3DC 0 /* 3-D compressible, src_compressible/ */
+#define LAPS_VARIANT_3DI 1 /* 3-D incompressible, src_incompressible/ */
+#define LAPS_VARIANT_2DC 2 /* 2-D compressible, src_compressible/2D/ */
+
+/* arithmetic of the transforms and the right-hand side */
+#define LAPS_PREC_FP64 0 /* native IEEE binary64 everywhere */
+#define LAPS_PREC_DD 1   /* float-float (two FP32, ~48-bit significand) on the FP32 pipes */
+#define LAPS_PREC_FP32 2 /* FP32 transforms and products, float-float RK accumulation */
+
+/* state layouts for laps_upload_state */
+#define LAPS_LAYOUT_PRIMITIVE 0 /* rho, ux, uy, uz, Bx, By, Bz, p (what outNNN.dat holds) */
+#define LAPS_LAYOUT_CONSERVED 1 /* rho, rho*ux, rho*uy, rho*uz, Bx, By, Bz, e */
+
+/*
+ * Namelist values the hot path reads.  Field names follow the reference's namelists
+ * (src_compressible/mhd.f90:30-41); defaults (laps_params_default) are the reference's
+ * module initialisers (mhdinit.f90:21-26, dealiasing.f90:10-12, mhd.f90:21, AEBmod.f90:10-12).
+ */
+typedef struct laps_params {
+  int variant;   /* LAPS_VARIANT_* */
+  int precision; /* LAPS_PREC_* */
+  int nx, ny, nz;
+  double Lx, Ly, Lz;
+  double adiabatic_index;
+  int if_resis, if_resis_exp;
+  double resistivity;
+  int if_visc, if_visc_exp;
+  double viscosity;
+  int if_conserve_background;
+  int dealias_option; /* 1: spherical 2/3 mask, 2: compact filter, other: none */
+  double afx, afy, afz;
+  double cfl;
+  int if_AEB;
+  double radius0, Ur0;
+  int if_corotating;
+  double corotating_angle;
+  int if_Hall;
+  double ion_inertial_length;
+  int device;             /* CUDA device ordinal */
+  int timeout_ms;         /* bound on every device wait (default 600000) */
+  long long mem_cap_bytes;/* refuse to allocate more than this (0: no cap) */
+  int reserved[8];
+} laps_params;
+
+typedef struct laps_ctx laps_ctx;
+
+/* Diagnostics of src_compressible/mhdrms.f90:53-126 and mhd.f90:522-570, plus the
+ * engine's own invariants (grid means). */
+typedef struct laps_diag {
+  double time, dt, radius;
+  double uu_ave[8];  /* <rho>, <ux>, <uy>, <uz>, <Bx>, <By>, <Bz>, <p>          */
+  double uu_rms[8];  /* <f^2> - <f>^2 for the same eight                         */
+  double rho_u2[3];  /* <rho (u_i - <u_i>)^2>                                    */
+  double max_divB;   /* max |i k . B_hat| over the spectral grid                 */
+  double e_kin;      /* <rho u^2>/2 */
+  double e_mag;      /* <B^2>/2     */
+  double h_cross;    /* <u . B>     */
+  double h_mag;      /* <A . B>, A_hat = i k x B_hat / k^2 (k != 0) */
+} laps_diag;
+
+typedef struct laps_info {
+  long long device_bytes; /* device memory held by the context */
+  int kx_keep, ky_keep, kz_keep; /* spectral extents the pruned passes touch */
+  int kernels_per_step;   /* kernel launches in one fused step */
+  int graph;              /* 1 when steps replay a captured CUDA graph */
+} laps_info;
+
+/* Fill *p with the reference's defaults. */
+int laps_params_default(laps_params* p);
+
+/* Allocate the device state for one run.  Replaces parallel_start / fftw_initialize /
+ * grid_initialize / arrays_initialize / AEB_initialize / dealias_initialize
+ * (src_compressible/mhd.f90:58-99; fftw.f90:21-39; mhdinit.f90:58-181; AEBmod.f90:16-44;
+ * dealiasing.f90:13-67). */
+int laps_create(const laps_params* p, laps_ctx** out);
+
+/* Free everything the context holds. */
+void laps_destroy(laps_ctx* ctx);
+
+/* Upload the state uu(nx,ny,nz,8) from the host, convert primitive -> conserved when asked,
+ * and transform it to Fourier space.  Replaces initial_calc_conserve_variable
+ * (mhdinit.f90:1038-1056) + transform_uu_real_to_fourier (fftw.f90:42-71, mhd.f90:121-122). */
+int laps_upload_state(laps_ctx* ctx, const double* uu, int layout);
+
+/* Set the simulation time and the expanding-box radius: evolve_radius(t)
+ * (AEBmod.f90:56-73,87-125), as the restart path does (mhd.f90:101-103). */
+int laps_set_time(laps_ctx* ctx, double time);
+
+/* CFL time step with the reference's +-2 % hysteresis against the current dt, then
+ * rkt_init: vardt (mhd.f90:328-429, rktmod.f90:15-32).  *dt receives the new dt. */
+int laps_vardt(laps_ctx* ctx, double* dt);
+
+/* Advance nsteps full steps.  Each step is vardt; evolve (three RK stages,
+ * mhd.f90:298-326); time += dt; evolve_radius(time) (mhd.f90:245-248) - the reference's
+ * loop body with its trailing vardt moved to the front.  A step whose dt is below 1e-8 is
+ * not taken and sets LAPS_STATUS_DT_FLOOR (mhd.f90:216).  On return *time and *dt hold the
+ * values after the last step and *status the OR of the status bits. */
+int laps_step(laps_ctx* ctx, int nsteps, double* time, double* dt, int* status);
+
+/* One RK stage irk = 1..3 of evolve with the current dt, for stage-level comparisons
+ * (mhd.f90:303-325: calc_flux, transform_flux_real_to_fourier, calc_rhs, rkt, dealias,
+ * transform_uu_fourier_to_real, update_uu_prim_from_uu). */
+int laps_rk_stage(laps_ctx* ctx, int irk);
+
+/* Inverse-transform the state and copy uu (conserved, nx*ny*nz*8) and uu_prim
+ * (ux, uy, uz, p: nx*ny*nz*4) to the host; either pointer may be NULL.  Replaces
+ * transform_uu_fourier_to_real + update_uu_prim_from_uu (fftw.f90:73-103,
+ * mhdrhs.f90:282-294) as used by output_uu (mhdoutput.f90:72-131). */
+int laps_download_state(laps_ctx* ctx, double* uu, double* uu_prim);
+
+/* Copy uu_fourier(nx/2+1,ny,nz,8) (interleaved complex float64) to / from the host. */
+int laps_download_spectral(laps_ctx* ctx, double* uf);
+int laps_upload_spectral(laps_ctx* ctx, const double* uf);
+
+/* Diagnostics: calc_rms (mhdrms.f90:53-126), calc_max_divB (mhd.f90:522-570), and the
+ * kinetic/magnetic energy, cross- and magnetic helicity of the current state. */
+int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
+
+/* Bounded wait for all queued work of the context. */
+int laps_wait(laps_ctx* ctx, int timeout_ms);
+
+/* Device-side time and dt. */
+int laps_get_time(laps_ctx* ctx, double* time, double* dt);
+
+int laps_get_info(laps_ctx* ctx, laps_info* info);
+
+/* Text of the last error on this context (or of the last failed laps_create when ctx is NULL). */
+const char* laps_last_error(laps_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LAPS_GPU_H */

@@ -1,0 +1,135 @@
+// C-ABI of the engine (declared in include/laps_gpu.h).  Every entry point converts
+// exceptions into LAPS_E* codes; nothing C++ crosses the boundary.
+#include <cstring>
+#include <new>
+#include <string>
+#include "engine_impl.cuh"
+
+namespace laps {
+EngineBase* make_engine_fp64(const laps_params& p);
+EngineBase* make_engine_dd(const laps_params& p);
+long long plan_bytes_fp64(const laps_params& p);
+long long plan_bytes_dd(const laps_params& p);
+}  // namespace laps
+
+struct laps_ctx {
+  laps::EngineBase* e = nullptr;
+  std::string err;
+};
+
+static thread_local std::string g_create_err;
+
+static int fail(laps_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  else g_create_err = m;
+  return code;
+}
+
+template <class F> static int guarded(laps_ctx* c, F f) {
+  if (!c || !c->e) return fail(c, LAPS_EINVAL, "null context");
+  try {
+    f();
+    return LAPS_OK;
+  } catch (const laps::Error& e) {
+    return fail(c, e.code, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(c, LAPS_ENOMEM, "host allocation failed");
+  } catch (...) {
+    return fail(c, LAPS_ECUDA, "unexpected error");
+  }
+}
+
+extern "C" {
+
+int laps_params_default(laps_params* p) {
+  if (!p) return LAPS_EINVAL;
+  std::memset(p, 0, sizeof(*p));
+  const double pi = 3.141592653589793;
+  p->variant = LAPS_VARIANT_3DC;
+  p->precision = LAPS_PREC_FP64;
+  p->nx = 128; p->ny = 128; p->nz = 64;  // mhdinit.f90:5
+  p->Lx = p->Ly = p->Lz = 2 * pi;
+  p->adiabatic_index = 5.0 / 3.0;      // mhdinit.f90:21
+  p->dealias_option = 2;               // dealiasing.f90:11
+  p->afx = p->afy = p->afz = 0.495;    // dealiasing.f90:12
+  p->cfl = 0.5;                        // mhd.f90:21
+  p->radius0 = 30.0;                   // AEBmod.f90:12
+  p->timeout_ms = 600000;
+  return LAPS_OK;
+}
+
+static bool size_ok(int n, int lo) { return n >= lo && n <= 512 && (n & (n - 1)) == 0; }
+
+int laps_create(const laps_params* p, laps_ctx** out) {
+  if (!p || !out) return fail(nullptr, LAPS_EINVAL, "null argument");
+  *out = nullptr;
+  if (p->variant != LAPS_VARIANT_3DC) return fail(nullptr, LAPS_EINVAL, "only the 3-D compressible variant is built in this library");
+  if (p->precision != LAPS_PREC_FP64 && p->precision != LAPS_PREC_DD)
+    return fail(nullptr, LAPS_EINVAL, "precision must be LAPS_PREC_FP64 or LAPS_PREC_DD");
+  if (!size_ok(p->nx, 16) || !size_ok(p->ny, 8) || !size_ok(p->nz, 8))
+    return fail(nullptr, LAPS_EINVAL, "nx must be a power of two in [16,512], ny and nz in [8,512]");
+  if (!(p->Lx > 0 && p->Ly > 0 && p->Lz > 0)) return fail(nullptr, LAPS_EINVAL, "box lengths must be positive");
+  if (!(p->adiabatic_index != 1.0) || !(p->cfl > 0)) return fail(nullptr, LAPS_EINVAL, "adiabatic_index must differ from 1 and cfl be positive");
+  if (p->if_AEB && !(p->radius0 > 0)) return fail(nullptr, LAPS_EINVAL, "radius0 must be positive");
+  long long need = p->precision == LAPS_PREC_FP64 ? laps::plan_bytes_fp64(*p) : laps::plan_bytes_dd(*p);
+  if (p->mem_cap_bytes > 0 && need > p->mem_cap_bytes)
+    return fail(nullptr, LAPS_ENOMEM, "device memory needed (" + std::to_string(need) + " bytes) exceeds mem_cap_bytes");
+  laps_ctx* c = new (std::nothrow) laps_ctx;
+  if (!c) return fail(nullptr, LAPS_ENOMEM, "host allocation failed");
+  try {
+    c->e = p->precision == LAPS_PREC_FP64 ? laps::make_engine_fp64(*p) : laps::make_engine_dd(*p);
+  } catch (const laps::Error& e) {
+    delete c;
+    return fail(nullptr, e.code, e.msg);
+  } catch (...) {
+    delete c;
+    return fail(nullptr, LAPS_ECUDA, "engine construction failed");
+  }
+  *out = c;
+  return LAPS_OK;
+}
+
+void laps_destroy(laps_ctx* c) {
+  if (!c) return;
+  delete c->e;
+  delete c;
+}
+
+int laps_upload_state(laps_ctx* c, const double* uu, int layout) {
+  if (!uu || (layout != LAPS_LAYOUT_PRIMITIVE && layout != LAPS_LAYOUT_CONSERVED)) return fail(c, LAPS_EINVAL, "bad state pointer or layout");
+  return guarded(c, [&] { c->e->upload(uu, layout); });
+}
+int laps_set_time(laps_ctx* c, double t) { return guarded(c, [&] { c->e->set_time(t); }); }
+int laps_vardt(laps_ctx* c, double* dt) {
+  return guarded(c, [&] {
+    double d = c->e->vardt();
+    if (dt) *dt = d;
+  });
+}
+int laps_step(laps_ctx* c, int n, double* time, double* dt, int* status) {
+  if (n < 0) return fail(c, LAPS_EINVAL, "nsteps < 0");
+  return guarded(c, [&] { c->e->step(n, time, dt, status); });
+}
+int laps_rk_stage(laps_ctx* c, int irk) { return guarded(c, [&] { c->e->rk_stage(irk); }); }
+int laps_download_state(laps_ctx* c, double* uu, double* prim) { return guarded(c, [&] { c->e->download(uu, prim); }); }
+int laps_download_spectral(laps_ctx* c, double* uf) {
+  if (!uf) return fail(c, LAPS_EINVAL, "null array");
+  return guarded(c, [&] { c->e->download_spectral(uf); });
+}
+int laps_upload_spectral(laps_ctx* c, const double* uf) {
+  if (!uf) return fail(c, LAPS_EINVAL, "null array");
+  return guarded(c, [&] { c->e->upload_spectral(uf); });
+}
+int laps_diagnostics(laps_ctx* c, laps_diag* d) {
+  if (!d) return fail(c, LAPS_EINVAL, "null diag");
+  return guarded(c, [&] { c->e->diagnostics(d); });
+}
+int laps_wait(laps_ctx* c, int timeout_ms) { return guarded(c, [&] { c->e->wait(timeout_ms); }); }
+int laps_get_time(laps_ctx* c, double* t, double* dt) { return guarded(c, [&] { c->e->get_time(t, dt); }); }
+int laps_get_info(laps_ctx* c, laps_info* i) {
+  if (!i) return fail(c, LAPS_EINVAL, "null info");
+  return guarded(c, [&] { c->e->info(i); });
+}
+const char* laps_last_error(laps_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+}  // extern "C"

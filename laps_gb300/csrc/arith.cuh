@@ -1,0 +1,208 @@
+// Arithmetic types of the engine: native FP64 (`double`), float-float (`dd`, an unevaluated
+// sum hi + lo of two FP32 values, ~48-bit significand, executed on the FP32 pipes), and FP32.
+//
+// On GB300 the FP64 pipe issues about 1.6 instructions/clock/SM against about 117 for FP32
+// FMA, so an FFT-based right-hand side in native FP64 is bound by the FP64 ALU, not by HBM.
+// `dd` trades ~10 FP32 instructions per FP64-equivalent operation for a 72x faster pipe.
+//
+// The float-float algorithms are the classical error-free transformations:
+//   two_sum (Knuth, TAOCP vol. 2, 4.2.2), fast_two_sum (Dekker 1971), two_prod via FMA,
+// assembled as in Hida, Li & Bailey, "Library for double-double and quad-double arithmetic"
+// (2007) ("sloppy" addition: its error is bounded relative to |a|+|b|, the norm-wise bound
+// FFT error analysis uses).  Every FP32 add here is an `__fadd_rn`/`__fsub_rn` intrinsic so
+// that the compiler cannot contract it into an FMA, which would break the error terms.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace laps {
+
+// ------------------------------------------------------------------------------ float-float
+struct dd {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dd dd_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ dd dd_fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+__device__ __forceinline__ dd operator+(dd a, dd b) {
+  dd s = dd_two_sum(a.hi, b.hi);
+  float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return dd_fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ dd operator-(dd a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return dd_fast_two_sum(p, e);
+}
+__device__ __forceinline__ dd dd_mul_f(dd a, float b) {
+  float p = __fmul_rn(a.hi, b);
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  return dd_fast_two_sum(p, e);
+}
+// exact scaling by a power of two
+__device__ __forceinline__ dd dd_ldexp(dd a, int e) { return {ldexpf(a.hi, e), ldexpf(a.lo, e)}; }
+__device__ __forceinline__ dd operator/(dd a, dd b) {
+  float q1 = __fdiv_rn(a.hi, b.hi);
+  dd r = a - dd_mul_f(b, q1);
+  float q2 = __fdiv_rn(r.hi, b.hi);
+  r = r - dd_mul_f(b, q2);
+  float q3 = __fdiv_rn(r.hi, b.hi);
+  dd q = dd_fast_two_sum(q1, q2);
+  return q + dd{q3, 0.f};
+}
+__device__ __forceinline__ dd dd_sqrt(dd a) {
+  if (!(a.hi > 0.f)) return {sqrtf(a.hi), 0.f};  // 0, negative (NaN) or NaN propagate
+  float s = __fsqrt_rn(a.hi);
+  // one Newton step in dd: s + (a - s^2) / (2 s)
+  float p = __fmul_rn(s, s);
+  float e = fmaf(s, s, -p);
+  dd sq = dd_fast_two_sum(p, e);
+  dd r = a - sq;
+  float c = __fdiv_rn(r.hi, __fmul_rn(2.f, s));
+  return dd_fast_two_sum(s, c);
+}
+__device__ __forceinline__ bool operator<(dd a, dd b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(dd a, dd b) { return b < a; }
+__device__ __forceinline__ dd dd_abs(dd a) { return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? -a : a; }
+
+// Host and device split of a double into a float-float (hi = nearest float, lo = rest).
+__host__ __device__ __forceinline__ dd dd_from_double(double d) {
+  float h = (float)d;
+  float l = (float)(d - (double)h);
+  return {h, l};
+}
+__host__ __device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
+
+// ------------------------------------------------------------------------------ traits
+// Real<T>: scalar ops used by generic code.  `cst(x)` turns a compile-time double into T.
+template <class T> struct Real;
+template <> struct Real<double> {
+  __device__ __forceinline__ static double cst(double x) { return x; }
+  __device__ __forceinline__ static double from_d(double x) { return x; }
+  __device__ __forceinline__ static double to_d(double x) { return x; }
+  __device__ __forceinline__ static double sqrt_(double x) { return sqrt(x); }
+  __device__ __forceinline__ static double abs_(double x) { return fabs(x); }
+  __device__ __forceinline__ static double max_(double a, double b) { return (a > b || a != a) ? a : b; }
+  __device__ __forceinline__ static double mul_pow2(double a, int e) { return ldexp(a, e); }
+  __device__ __forceinline__ static float lead(double x) { return (float)x; }
+  __device__ __forceinline__ static bool isnan_(double x) { return x != x; }
+  __device__ __forceinline__ static double min_(double a, double b) { return b < a ? b : a; }
+  __device__ __forceinline__ static double inf() { return __longlong_as_double(0x7FF0000000000000ll); }
+};
+template <> struct Real<dd> {
+  __device__ __forceinline__ static dd cst(double x) { return dd_from_double(x); }
+  __device__ __forceinline__ static dd from_d(double x) { return dd_from_double(x); }
+  __device__ __forceinline__ static double to_d(dd x) { return dd_to_double(x); }
+  __device__ __forceinline__ static dd sqrt_(dd x) { return dd_sqrt(x); }
+  __device__ __forceinline__ static dd abs_(dd x) { return dd_abs(x); }
+  __device__ __forceinline__ static dd max_(dd a, dd b) { return (a > b || a.hi != a.hi) ? a : b; }
+  __device__ __forceinline__ static dd mul_pow2(dd a, int e) { return dd_ldexp(a, e); }
+  __device__ __forceinline__ static float lead(dd x) { return x.hi; }
+  __device__ __forceinline__ static bool isnan_(dd x) { return x.hi != x.hi; }
+  __device__ __forceinline__ static dd min_(dd a, dd b) { return b < a ? b : a; }
+  __device__ __forceinline__ static dd inf() { return {__int_as_float(0x7f800000), 0.f}; }
+};
+template <> struct Real<float> {
+  __device__ __forceinline__ static float cst(double x) { return (float)x; }
+  __device__ __forceinline__ static float from_d(double x) { return (float)x; }
+  __device__ __forceinline__ static double to_d(float x) { return (double)x; }
+  __device__ __forceinline__ static float sqrt_(float x) { return sqrtf(x); }
+  __device__ __forceinline__ static float abs_(float x) { return fabsf(x); }
+  __device__ __forceinline__ static float max_(float a, float b) { return (a > b || a != a) ? a : b; }
+  __device__ __forceinline__ static float mul_pow2(float a, int e) { return ldexpf(a, e); }
+  __device__ __forceinline__ static float lead(float x) { return x; }
+  __device__ __forceinline__ static bool isnan_(float x) { return x != x; }
+  __device__ __forceinline__ static float min_(float a, float b) { return b < a ? b : a; }
+  __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
+};
+
+// ------------------------------------------------------------------------------ complex
+template <class T> struct cx {
+  T re, im;
+};
+template <class T> __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <class T> __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return {a.re - b.re, a.im - b.im}; }
+template <class T> __device__ __forceinline__ cx<T> operator-(cx<T> a) { return {-a.re, -a.im}; }
+template <class T> __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <class T> __device__ __forceinline__ cx<T> operator*(cx<T> a, T s) { return {a.re * s, a.im * s}; }
+template <class T> __device__ __forceinline__ cx<T> conj(cx<T> a) { return {a.re, -a.im}; }
+// multiply by i * s  (the spectral derivative with real wave number s)
+template <class T> __device__ __forceinline__ cx<T> mul_i(cx<T> a, T s) { return {-(a.im * s), a.re * s}; }
+// multiply by +i or -i
+template <class T> __device__ __forceinline__ cx<T> times_i(cx<T> a) { return {-a.im, a.re}; }
+template <class T> __device__ __forceinline__ cx<T> times_mi(cx<T> a) { return {a.im, -a.re}; }
+template <class T> __device__ __forceinline__ cx<T> cx_zero() { return {Real<T>::cst(0.0), Real<T>::cst(0.0)}; }
+
+// Complex float-float product with shared error terms (~36 FP32 instructions instead of 50).
+__device__ __forceinline__ cx<dd> operator*(cx<dd> a, cx<dd> b) {
+  // re = a.re*b.re - a.im*b.im ; im = a.re*b.im + a.im*b.re
+  float p1 = __fmul_rn(a.re.hi, b.re.hi), p2 = __fmul_rn(a.im.hi, b.im.hi);
+  float e1 = fmaf(a.re.hi, b.re.hi, -p1), e2 = fmaf(a.im.hi, b.im.hi, -p2);
+  dd s = dd_two_sum(p1, -p2);
+  float e = __fadd_rn(s.lo, __fsub_rn(e1, e2));
+  e = fmaf(a.re.hi, b.re.lo, e);
+  e = fmaf(a.re.lo, b.re.hi, e);
+  e = fmaf(-a.im.hi, b.im.lo, e);
+  e = fmaf(-a.im.lo, b.im.hi, e);
+  dd re = dd_fast_two_sum(s.hi, e);
+  float q1 = __fmul_rn(a.re.hi, b.im.hi), q2 = __fmul_rn(a.im.hi, b.re.hi);
+  float f1 = fmaf(a.re.hi, b.im.hi, -q1), f2 = fmaf(a.im.hi, b.re.hi, -q2);
+  dd t = dd_two_sum(q1, q2);
+  float f = __fadd_rn(t.lo, __fadd_rn(f1, f2));
+  f = fmaf(a.re.hi, b.im.lo, f);
+  f = fmaf(a.re.lo, b.im.hi, f);
+  f = fmaf(a.im.hi, b.re.lo, f);
+  f = fmaf(a.im.lo, b.re.hi, f);
+  dd im = dd_fast_two_sum(t.hi, f);
+  return {re, im};
+}
+
+// ------------------------------------------------------------------------------ storage
+// How a value of type T lives in memory.  Complex values are one 16-byte (FP64, dd) or
+// 8-byte (FP32) vector so that a quarter-warp moves one 128-byte row per instruction.
+template <class T> struct Store;
+template <> struct Store<double> {
+  using R = double;
+  using C = double2;
+  __device__ __forceinline__ static double ld(const R* p) { return *p; }
+  __device__ __forceinline__ static void st(R* p, double v) { *p = v; }
+  __device__ __forceinline__ static cx<double> ldc(const C* p) { C v = *p; return {v.x, v.y}; }
+  __device__ __forceinline__ static cx<double> ldg(const C* p) { C v = __ldg(p); return {v.x, v.y}; }
+  __device__ __forceinline__ static void stc(C* p, cx<double> v) { *p = make_double2(v.re, v.im); }
+};
+template <> struct Store<dd> {
+  using R = float2;
+  using C = float4;
+  __device__ __forceinline__ static dd ld(const R* p) { R v = *p; return {v.x, v.y}; }
+  __device__ __forceinline__ static void st(R* p, dd v) { *p = make_float2(v.hi, v.lo); }
+  __device__ __forceinline__ static cx<dd> ldc(const C* p) { C v = *p; return {{v.x, v.y}, {v.z, v.w}}; }
+  __device__ __forceinline__ static cx<dd> ldg(const C* p) { C v = __ldg(p); return {{v.x, v.y}, {v.z, v.w}}; }
+  __device__ __forceinline__ static void stc(C* p, cx<dd> v) { *p = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo); }
+};
+template <> struct Store<float> {
+  using R = float;
+  using C = float2;
+  __device__ __forceinline__ static float ld(const R* p) { return *p; }
+  __device__ __forceinline__ static void st(R* p, float v) { *p = v; }
+  __device__ __forceinline__ static cx<float> ldc(const C* p) { C v = *p; return {v.x, v.y}; }
+  __device__ __forceinline__ static cx<float> ldg(const C* p) { C v = __ldg(p); return {v.x, v.y}; }
+  __device__ __forceinline__ static void stc(C* p, cx<float> v) { *p = make_float2(v.re, v.im); }
+};
+
+}  // namespace laps

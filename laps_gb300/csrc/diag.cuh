@@ -1,0 +1,116 @@
+// Diagnostics reductions: calc_rms (src_compressible/mhdrms.f90:53-126), calc_max_divB
+// (src_compressible/mhd.f90:522-570), and the engine's energy / cross-helicity /
+// magnetic-helicity sums.  Each block writes its partial results; the host adds the
+// partials in block order, so repeated calls give bitwise-identical results.
+#pragma once
+#include "kernels.cuh"
+
+namespace laps {
+
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* out) {
+  __shared__ double red[8][NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+    for (int k = 0; k < NV; k++) red[w][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i][threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+// sums of rho, ux, uy, uz, Bx, By, Bz, p, their squares, rho u^2, B^2 and u.B
+template <class T>
+__global__ void __launch_bounds__(256) k_diag_sums(const typename Store<T>::R* __restrict__ u, long long n, double gamma,
+                                                   double* part) {
+  double v[19];
+#pragma unroll
+  for (int k = 0; k < 19; k++) v[k] = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double q[8];
+#pragma unroll
+    for (int f = 0; f < 8; f++) q[f] = Real<T>::to_d(Store<T>::ld(u + f * n + i));
+    double ux = q[1] / q[0], uy = q[2] / q[0], uz = q[3] / q[0];
+    double p = (q[7] - 0.5 * (q[1] * ux + q[2] * uy + q[3] * uz + q[4] * q[4] + q[5] * q[5] + q[6] * q[6])) * (gamma - 1);
+    double f8[8] = {q[0], ux, uy, uz, q[4], q[5], q[6], p};
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      v[k] += f8[k];
+      v[8 + k] += f8[k] * f8[k];
+    }
+    v[16] += q[0] * (ux * ux + uy * uy + uz * uz);
+    v[17] += q[4] * q[4] + q[5] * q[5] + q[6] * q[6];
+    v[18] += ux * q[4] + uy * q[5] + uz * q[6];
+  }
+  block_sum<19>(v, part + (size_t)blockIdx.x * 32);
+}
+
+// sum of rho (u_i - <u_i>)^2 (mhdrms.f90:110-125)
+template <class T>
+__global__ void __launch_bounds__(256) k_diag_rhou2(const typename Store<T>::R* __restrict__ u, long long n, double a1, double a2,
+                                                    double a3, double* part) {
+  double v[3] = {0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double rho = Real<T>::to_d(Store<T>::ld(u + i));
+    double ux = Real<T>::to_d(Store<T>::ld(u + n + i)) / rho;
+    double uy = Real<T>::to_d(Store<T>::ld(u + 2 * n + i)) / rho;
+    double uz = Real<T>::to_d(Store<T>::ld(u + 3 * n + i)) / rho;
+    v[0] += rho * (ux - a1) * (ux - a1);
+    v[1] += rho * (uy - a2) * (uy - a2);
+    v[2] += rho * (uz - a3) * (uz - a3);
+  }
+  block_sum<3>(v, part + (size_t)blockIdx.x * 8);
+}
+
+// max |i k.B| and <A.B> with A = i k x B / |k|^2 from the half spectrum (Parseval weights:
+// 2 for 0 < kx < nx/2, else 1)
+template <class T>
+__global__ void __launch_bounds__(256) k_diag_spec(const typename Store<T>::C* __restrict__ U, Geo g, KTab<T> K, Phys P, PT<T> pc,
+                                                   const StepState* st, double* part) {
+  double mx = 0.0, hm = 0.0;
+  long long tot = (long long)g.nz * g.ny * g.nh;
+  T rr = Real<T>::from_d(st->r_ratio);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    int kx = i % g.nh;
+    long long r = i / g.nh;
+    int ky = r % g.ny, kz = r / g.ny;
+    long long idx = (long long)kz * g.ny * g.kxp + (long long)ky * g.kxp + kx;
+    T axT, ayT, azT;
+    kfac(K, P, pc, rr, kx, ky, kz, axT, ayT, azT);
+    double ax = Real<T>::to_d(axT), ay = Real<T>::to_d(ayT), az = Real<T>::to_d(azT);
+    cx<T> bxT = Store<T>::ldc(U + 4 * g.fsc + idx), byT = Store<T>::ldc(U + 5 * g.fsc + idx), bzT = Store<T>::ldc(U + 6 * g.fsc + idx);
+    double bxr = Real<T>::to_d(bxT.re), bxi = Real<T>::to_d(bxT.im);
+    double byr = Real<T>::to_d(byT.re), byi = Real<T>::to_d(byT.im);
+    double bzr = Real<T>::to_d(bzT.re), bzi = Real<T>::to_d(bzT.im);
+    // i (ax Bx + ay By + az Bz)
+    double dr = ax * bxr + ay * byr + az * bzr, di = ax * bxi + ay * byi + az * bzi;
+    mx = fmax(mx, hypot(dr, di));
+    double k2 = ax * ax + ay * ay + az * az;
+    if (k2 > 0.0) {
+      // c = k x B ; A = i c / k2 ; Re(A . conj B) = -Im(c . conj B) / k2
+      double cxr = ay * bzr - az * byr, cxi = ay * bzi - az * byi;
+      double cyr = az * bxr - ax * bzr, cyi = az * bxi - ax * bzi;
+      double czr = ax * byr - ay * bxr, czi = ax * byi - ay * bxi;
+      double im = (cxi * bxr - cxr * bxi) + (cyi * byr - cyr * byi) + (czi * bzr - czr * bzi);
+      double w = (kx == 0 || 2 * kx == g.nx) ? 1.0 : 2.0;
+      hm += -w * im / k2;
+    }
+  }
+  __shared__ double rm[8];
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) rm[threadIdx.x >> 5] = mx;
+  double v[1] = {hm};
+  block_sum<1>(v, part + (size_t)blockIdx.x * 2 + 1);
+  if (threadIdx.x == 0) {
+    double m = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = fmax(m, rm[i]);
+    part[(size_t)blockIdx.x * 2] = m;
+  }
+}
+
+}  // namespace laps

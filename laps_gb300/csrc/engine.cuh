@@ -1,0 +1,103 @@
+// Device-side definitions shared by every kernel of the engine: grid geometry, the
+// per-step scalars that live in device memory (so a captured step needs no host input),
+// wave-number tables and the pointwise physics of the 3-D compressible equations.
+#pragma once
+#include "fft.cuh"
+#include "../../include/laps_gpu.h"
+
+namespace laps {
+
+constexpr int TX = 8;  // columns per tile: 8 x 16 B = one 128-byte row
+
+// ------------------------------------------------------------------------------ geometry
+// Spectral / intermediate arrays: field-major, then z, y, and kx fastest with a row pitch
+// kxp = round_up(nx/2+1, 8), i.e. the reference's uu_fourier(kx,ky,kz,ivar) order
+// (src_compressible/mhdinit.f90:155-169) with padded rows.  Real arrays: (x, y, z, field)
+// exactly as the reference's uu(ix,iy,iz,ivar).
+struct Geo {
+  int nx, ny, nz, nh;     // nh = nx/2 + 1
+  int kxp;                // spectral row pitch
+  long long fsc;          // complex field stride = nz*ny*kxp
+  long long fsr;          // real field stride = nz*ny*nx
+  // kept (non-zero) spectral ranges: kx < kx_keep, ky in [0,ky_lo) U [ky_hi,ny), same for kz
+  int kx_keep, ky_lo, ky_hi, kz_lo, kz_hi;
+  __host__ __device__ int nky() const { return ky_lo + (ny - ky_hi); }
+  __host__ __device__ int nkz() const { return kz_lo + (nz - kz_hi); }
+  __host__ __device__ int ky_of(int r) const { return r < ky_lo ? r : ky_hi + (r - ky_lo); }
+  __host__ __device__ int kz_of(int r) const { return r < kz_lo ? r : kz_hi + (r - kz_lo); }
+  __host__ __device__ bool ky_in(int ky) const { return ky < ky_lo || ky >= ky_hi; }
+  __host__ __device__ bool kz_in(int kz) const { return kz < kz_lo || kz >= kz_hi; }
+};
+
+// ------------------------------------------------------------------------------ step state
+// Written only by device kernels during a step; read by every pass kernel.
+struct StepState {
+  double time, dt, radius;
+  double cc[3], ddc[3], ts[3];     // RK3 coefficients of rktmod.f90:17-27 times dt
+  double inv_tau;                  // 1 / tau_exp (0 when the expanding box is off)
+  double r_ratio;                  // radius0 / radius
+  unsigned long long cfl_bits;     // running min of the CFL time step (bits of a double)
+  int status;                      // LAPS_STATUS_* bits
+  int halt;                        // skip the rest of the step (dt floor)
+  int ksq_plain;                   // k^2 still the grid_initialize sum (no R factor)
+  int pad;
+};
+
+// wave-number tables (element type T), rebuilt by a small kernel whenever R changes
+template <class T> struct KTab {
+  const T* wx;   // kx (nh)
+  const T* wy;   // ky (ny) unscaled
+  const T* kyd;  // ky * R0 / R   (derivative factor)
+  const T* kzd;  // kz * R0 / R
+  const T* kx2;  // terms of k^2: kx^2, (ky R0/R)^2, (kz R0/R)^2 (plain squares before the first R update)
+  const T* ky2;
+  const T* kz2;
+  const T* fx;   // dealias option 2 filters (or null)
+  const T* fy;
+  const T* fz;
+  const short* kxlim;  // dealias option 1: number of kept kx for each (kz, ky) row, or null
+};
+
+// scalar physics parameters, by value
+struct Phys {
+  double gamma, nu, eta, di, cfl, dx, dy, dz, mindx, R0, Ur;
+  double cos_cor, sin_cor;
+  // corotating k^2 coefficients (set per step from R0/R)
+  int visc, visc_exp, resis, resis_exp, cons_bg, aeb, corot, hall, dealias;
+};
+
+// the same constants pre-converted to T on the host (a double -> float-float split per
+// element would run on the FP64 pipe)
+template <class T> struct PT {
+  T gamma, gm1, cg, di, nu, eta, cosc, sinc, inv_mindx, half, two, one, zero, four, is2, dx, dy, dz;
+  T ebm[8];
+};
+
+// effective derivative factors (i*ax, i*ay, i*az) at spectral index (ix, iy, iz):
+// src_compressible/mhdrhs.f90:191-204 (corotation mixes kx and ky)
+template <class T>
+__device__ __forceinline__ void kfac(const KTab<T>& K, const Phys& P, const PT<T>& c, T rr, int ix, int iy, int iz, T& ax, T& ay, T& az) {
+  az = K.kzd[iz];
+  if (P.corot) {
+    ax = K.wx[ix] * c.cosc + K.wy[iy] * c.sinc;
+    ay = (K.wy[iy] * c.cosc - K.wx[ix] * c.sinc) * rr;
+  } else {
+    ax = K.wx[ix];
+    ay = K.kyd[iy];
+  }
+}
+
+// k^2 at (ix, iy, iz): src_compressible/AEBmod.f90:87-125 and mhdinit.f90:117-123
+template <class T>
+__device__ __forceinline__ T ksq(const KTab<T>& K, const Phys& P, const PT<T>& q, T rr, int ix, int iy, int iz) {
+  if (P.corot) {
+    T c = q.cosc, s = q.sinc;
+    T kx = K.wx[ix], ky = K.wy[iy];
+    T r2 = rr * rr;
+    T sr = s * rr, cr = c * rr;
+    return kx * kx * (c * c + sr * sr) + ky * ky * (s * s + cr * cr) + kx * ky * q.two * c * s * (q.one - r2) + K.kz2[iz];
+  }
+  return (K.kx2[ix] + K.ky2[iy]) + K.kz2[iz];
+}
+
+}  // namespace laps

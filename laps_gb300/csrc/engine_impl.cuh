@@ -1,0 +1,524 @@
+// Host side of the engine: parameter checks, device allocation, tables, kernel dispatch
+// over the supported line lengths, the fused step (captured once into a CUDA graph and
+// replayed), transforms for upload / download, and diagnostics.
+#pragma once
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <chrono>
+#include <thread>
+#include "launch.cuh"
+#include "diag.cuh"
+
+namespace laps {
+
+
+// ---------------------------------------------------------------------------- host conversions
+template <class T> T host_cvt(long double x);
+template <> inline double host_cvt<double>(long double x) { return (double)x; }
+template <> inline float host_cvt<float>(long double x) { return (float)x; }
+template <> inline dd host_cvt<dd>(long double x) {
+  float h = (float)x;
+  float l = (float)(x - (long double)h);
+  return {h, l};
+}
+template <class T> typename Store<T>::C host_cplx(long double re, long double im);
+template <> inline double2 host_cplx<double>(long double re, long double im) { return make_double2((double)re, (double)im); }
+template <> inline float2 host_cplx<float>(long double re, long double im) { return make_float2((float)re, (float)im); }
+template <> inline float4 host_cplx<dd>(long double re, long double im) {
+  dd a = host_cvt<dd>(re), b = host_cvt<dd>(im);
+  return make_float4(a.hi, a.lo, b.hi, b.lo);
+}
+
+// exp(-2 pi i j / n), j = 0..n-1
+template <class T> std::vector<typename Store<T>::C> twiddles(int n) {
+  std::vector<typename Store<T>::C> t(n);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int j = 0; j < n; j++) {
+    long double a = 2.0L * pi * (long double)j / (long double)n;
+    t[j] = host_cplx<T>(cosl(a), -sinl(a));
+  }
+  return t;
+}
+
+class EngineBase {
+ public:
+  virtual ~EngineBase() {}
+  virtual void upload(const double* h, int layout) = 0;
+  virtual void set_time(double t) = 0;
+  virtual double vardt() = 0;
+  virtual void step(int n, double* time, double* dt, int* status) = 0;
+  virtual void rk_stage(int irk) = 0;
+  virtual void download(double* uu, double* prim) = 0;
+  virtual void download_spectral(double* uf) = 0;
+  virtual void upload_spectral(const double* uf) = 0;
+  virtual void diagnostics(laps_diag* d) = 0;
+  virtual void wait(int timeout_ms) = 0;
+  virtual void get_time(double* t, double* dt) = 0;
+  virtual void info(laps_info* i) = 0;
+};
+
+template <class T> class Engine : public EngineBase {
+  using C = typename Store<T>::C;
+  using SR = typename Store<T>::R;
+
+ public:
+  laps_params p;
+  Geo gfull, gprune;
+  Phys P;
+  PT<T> pc;
+  bool prune_ok = false;   // dealias option 1: the box |k_i| <= n_i/3 holds every non-zero mode
+  bool dealiased = false;  // the state has been through at least one RK stage since upload
+  bool have_state = false;
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph_steady = nullptr;
+  long long bytes = 0;
+  std::vector<void*> allocs;
+  Bufs<T> B{};
+  C *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  SR *t_wx, *t_wy, *t_kyd, *t_kzd, *t_kx2, *t_ky2, *t_kz2, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr;
+  double *d_wx, *d_wy, *d_wz;
+  short* kxlim = nullptr;
+  StepState* st = nullptr;
+  StepState* h_st = nullptr;  // pinned mirror
+  double* d_part = nullptr;   // diagnostics partial sums
+  int npart = 0;
+
+  template <class X> X* dalloc(size_t n) {
+    void* ptr = nullptr;
+    LAPS_CK(cudaMalloc(&ptr, n * sizeof(X)));
+    allocs.push_back(ptr);
+    return (X*)ptr;
+  }
+
+  static long long plan_bytes(const laps_params& q) {
+    long long kxp = ((q.nx / 2 + 1) + 7) / 8 * 8;
+    long long fsc = kxp * q.ny * q.nz;
+    return (8 + 8 + 19 + 15) * fsc * (long long)sizeof(C) + (1 << 20);
+  }
+
+  explicit Engine(const laps_params& q) : p(q) {
+    dev = q.device;
+    LAPS_CK(cudaSetDevice(dev));
+    Geo g{};
+    g.nx = q.nx; g.ny = q.ny; g.nz = q.nz; g.nh = q.nx / 2 + 1;
+    g.kxp = (g.nh + 7) / 8 * 8;
+    g.fsc = (long long)g.kxp * g.ny * g.nz;
+    g.fsr = (long long)g.nx * g.ny * g.nz;
+    g.kx_keep = g.nh; g.ky_lo = g.ny; g.ky_hi = g.ny; g.kz_lo = g.nz; g.kz_hi = g.nz;
+    gfull = g;
+    // physics scalars
+    const double pi = 3.141592653589793;
+    P = Phys{};
+    P.gamma = q.adiabatic_index;
+    P.nu = q.viscosity; P.eta = q.resistivity; P.di = q.ion_inertial_length; P.cfl = q.cfl;
+    P.dx = q.Lx / q.nx; P.dy = q.Ly / q.ny; P.dz = q.Lz / q.nz;
+    P.mindx = std::fmin(std::fmin(P.dx, P.dy), P.dz);
+    P.R0 = q.radius0;
+    P.Ur = q.if_AEB ? q.Ur0 : 0.0;  // mhd.f90:88-90
+    double ang = q.if_corotating ? q.corotating_angle : 0.0;  // AEBmod.f90:28-30
+    P.cos_cor = std::cos(ang); P.sin_cor = std::sin(ang);
+    P.visc = q.if_visc; P.visc_exp = q.if_visc_exp; P.resis = q.if_resis; P.resis_exp = q.if_resis_exp;
+    P.cons_bg = q.if_conserve_background; P.aeb = q.if_AEB; P.corot = q.if_AEB && q.if_corotating;
+    P.hall = q.if_Hall; P.dealias = (q.dealias_option == 1 || q.dealias_option == 2) ? q.dealias_option : 0;
+    pc.gamma = host_cvt<T>(P.gamma); pc.gm1 = host_cvt<T>(P.gamma - 1.0);
+    pc.cg = host_cvt<T>(-2.0 * P.gamma / (P.gamma - 1.0));
+    pc.di = host_cvt<T>(P.di); pc.nu = host_cvt<T>(P.nu); pc.eta = host_cvt<T>(P.eta);
+    pc.cosc = host_cvt<T>(P.cos_cor); pc.sinc = host_cvt<T>(P.sin_cor);
+    pc.inv_mindx = host_cvt<T>(1.0 / P.mindx);
+    pc.half = host_cvt<T>(0.5); pc.two = host_cvt<T>(2.0); pc.one = host_cvt<T>(1.0);
+    pc.zero = host_cvt<T>(0.0); pc.four = host_cvt<T>(4.0);
+    pc.is2 = host_cvt<T>(0.70710678118654752440L);
+    pc.dx = host_cvt<T>(P.dx); pc.dy = host_cvt<T>(P.dy); pc.dz = host_cvt<T>(P.dz);
+    const double ebm[8] = {2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 0.0};  // mhdrhs.f90:237-247
+    for (int v = 0; v < 8; v++) pc.ebm[v] = host_cvt<T>(ebm[v]);
+
+    // wave numbers, mhdinit.f90:88-115 (the Nyquist index takes +k)
+    auto wn = [&](int n, double L) {
+      std::vector<double> w(n);
+      for (int i = 1; i <= n; i++) w[i - 1] = (i <= n / 2 + 1) ? 2 * pi * (i - 1) / L : 2 * pi * (i - 1 - n) / L;
+      return w;
+    };
+    std::vector<double> wx = wn(q.nx, q.Lx), wy = wn(q.ny, q.Ly), wz = wn(q.nz, q.Lz);
+    wx.resize(g.nh);
+
+    // dealias option 1: kept kx count per (kz, ky) row with the reference's own formula
+    // (dealiasing.f90:87-99), and the box that holds every kept mode
+    std::vector<short> lim;
+    if (P.dealias == 1) {
+      lim.assign((size_t)q.nz * q.ny, 0);
+      int kxk = 0, kyk = 0, kzk = 0;
+      for (int iz = 0; iz < q.nz; iz++)
+        for (int iy = 0; iy < q.ny; iy++) {
+          int cnt = 0;
+          for (int ix = 0; ix < g.nh; ix++) {
+            double r = std::sqrt(std::pow(wx[ix] * q.Lx / (2 * pi * q.nx), 2) + std::pow(wy[iy] * q.Ly / (2 * pi * q.ny), 2) +
+                                 std::pow(wz[iz] * q.Lz / (2 * pi * q.nz), 2));
+            if (!(r > 1.0 / 3.0)) {
+              if (cnt != ix) throw Error{LAPS_EINVAL, "dealias mask is not monotone in kx"};
+              cnt = ix + 1;
+              int my = iy <= q.ny / 2 ? iy : q.ny - iy, mz = iz <= q.nz / 2 ? iz : q.nz - iz;
+              kxk = std::max(kxk, ix);
+              kyk = std::max(kyk, my);
+              kzk = std::max(kzk, mz);
+            }
+          }
+          lim[(size_t)iz * q.ny + iy] = (short)cnt;
+        }
+      Geo gp = g;
+      gp.kx_keep = kxk + 1;
+      if (2 * kyk + 1 < q.ny) { gp.ky_lo = kyk + 1; gp.ky_hi = q.ny - kyk; }
+      if (2 * kzk + 1 < q.nz) { gp.kz_lo = kzk + 1; gp.kz_hi = q.nz - kzk; }
+      gprune = gp;
+      prune_ok = true;
+    } else {
+      gprune = g;
+    }
+
+    LAPS_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    B.U = dalloc<C>(8 * g.fsc);
+    B.R = dalloc<C>(8 * g.fsc);
+    B.W1 = dalloc<C>(19 * g.fsc);
+    B.W2 = dalloc<C>(15 * g.fsc);
+    bytes = (8 + 8 + 19 + 15) * g.fsc * (long long)sizeof(C);
+    LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(C), stream));
+    LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
+    auto up = [&](auto* dst, const auto& src) {
+      LAPS_CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
+    };
+    auto twx_h = twiddles<T>(q.nx), twy_h = twiddles<T>(q.ny), twz_h = twiddles<T>(q.nz);
+    twx = dalloc<C>(q.nx); up(twx, twx_h);
+    twy = dalloc<C>(q.ny); up(twy, twy_h);
+    twz = dalloc<C>(q.nz); up(twz, twz_h);
+    d_wx = dalloc<double>(g.nh); up(d_wx, wx);
+    d_wy = dalloc<double>(q.ny); up(d_wy, wy);
+    d_wz = dalloc<double>(q.nz); up(d_wz, wz);
+    t_wx = dalloc<SR>(g.nh); t_kx2 = dalloc<SR>(g.nh);
+    t_wy = dalloc<SR>(q.ny); t_kyd = dalloc<SR>(q.ny); t_ky2 = dalloc<SR>(q.ny);
+    t_kzd = dalloc<SR>(q.nz); t_kz2 = dalloc<SR>(q.nz);
+    if (P.dealias == 1) { kxlim = dalloc<short>(lim.size()); up(kxlim, lim); }
+    if (P.dealias == 2) {  // dealiasing.f90:31-65
+      auto filt = [&](const std::vector<double>& w, double L, int n, double af) {
+        double aj = (5.0 + 6.0 * af) / 8.0, bj = (1.0 + 2.0 * af) / 2.0, cj = -(1.0 - 2 * af) / 8.0;
+        std::vector<SR> f(w.size());
+        for (size_t i = 0; i < w.size(); i++) {
+          double wl = w[i] * L / n;
+          double v = (aj + bj * std::cos(wl) + cj * std::cos(2 * wl)) / (1 + 2 * af * std::cos(wl));
+          T tv = host_cvt<T>(v);
+          std::memcpy(&f[i], &tv, sizeof(SR));
+        }
+        return f;
+      };
+      auto fx = filt(wx, q.Lx, q.nx, q.afx), fy = filt(wy, q.Ly, q.ny, q.afy), fz = filt(wz, q.Lz, q.nz, q.afz);
+      t_fx = dalloc<SR>(fx.size()); up(t_fx, fx);
+      t_fy = dalloc<SR>(fy.size()); up(t_fy, fy);
+      t_fz = dalloc<SR>(fz.size()); up(t_fz, fz);
+    }
+    st = dalloc<StepState>(1);
+    LAPS_CK(cudaMallocHost(&h_st, sizeof(StepState)));
+    StepState s0{};
+    s0.time = 0.0; s0.dt = 0.0; s0.radius = q.radius0;
+    s0.inv_tau = P.Ur != 0.0 ? 1.0 / (q.radius0 / P.Ur) : 0.0;
+    s0.r_ratio = 1.0;  // radius0 / radius at start; the factor itself is (k R0)/R below
+    s0.cfl_bits = 0x7FF0000000000000ull;
+    s0.ksq_plain = 1;  // grid_initialize's k^2 until the first evolve_radius
+    LAPS_CK(cudaMemcpy(st, &s0, sizeof(s0), cudaMemcpyHostToDevice));
+    npart = 4096;
+    d_part = dalloc<double>((size_t)npart * 32);
+    tables();
+    LAPS_CK(cudaStreamSynchronize(stream));
+  }
+
+  ~Engine() override {
+    if (graph_steady) cudaGraphExecDestroy(graph_steady);
+    for (void* a : allocs) cudaFree(a);
+    if (h_st) cudaFreeHost(h_st);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  KTab<T> ktab() const {
+    KTab<T> K;
+    K.wx = (const T*)t_wx; K.wy = (const T*)t_wy; K.kyd = (const T*)t_kyd; K.kzd = (const T*)t_kzd;
+    K.kx2 = (const T*)t_kx2; K.ky2 = (const T*)t_ky2; K.kz2 = (const T*)t_kz2;
+    K.fx = (const T*)t_fx; K.fy = (const T*)t_fy; K.fz = (const T*)t_fz;
+    K.kxlim = kxlim;
+    return K;
+  }
+
+  void tables() {
+    k_tables<T><<<1, 256, 0, stream>>>(d_wx, d_wy, d_wz, t_wx, t_wy, t_kyd, t_kzd, t_kx2, t_ky2, t_kz2, gfull.nh, p.ny, p.nz,
+                                       p.radius0, st);
+    LAPS_CK(cudaGetLastError());
+  }
+
+  // ---------------------------------------------------------------- plain transforms
+  void col_plain(const C* in, C* out, int nf, int N, int dir, int jstride, int ostride, int ncol, int nouter, int sexp,
+                 const C* tw) {
+    launch_col_plain<T>(stream, in, out, gfull.fsc, nf, N, dir, jstride, ostride, ncol, nouter, sexp, tw);
+  }
+  void rows_r2c(const SR* in, C* out, long long nrows) { launch_rows_r2c<T>(stream, p.nx, in, out, nrows, gfull.kxp, twx); }
+  void rows_c2r(const C* in, SR* out, long long nrows) { launch_rows_c2r<T>(stream, p.nx, in, out, nrows, gfull.kxp, twx); }
+  // real T fields (W1 layout, nf) -> spectrum `out` (fsc pitch)
+  void forward3d(const SR* real, C* out, int nf) {
+    const Geo& g = gfull;
+    rows_r2c(real, B.W2, (long long)nf * g.ny * g.nz);
+    for (int f = 0; f < nf; f++) {
+      // y: element (f, z, y, kx): jstride = kxp, outer = z with ostride ny*kxp
+      col_plain(B.W2 + f * g.fsc, B.W2 + f * g.fsc, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twy);
+      // z: jstride = ny*kxp, outer = y with ostride kxp
+      col_plain(B.W2 + f * g.fsc, out + f * g.fsc, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twz);
+    }
+  }
+  // spectrum (nf fields) -> real T fields in W1
+  void inverse3d(const C* spec, int nf) {
+    const Geo& g = gfull;
+    for (int f = 0; f < nf; f++) {
+      col_plain(spec + f * g.fsc, B.W2 + f * g.fsc, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twz);
+      col_plain(B.W2 + f * g.fsc, B.W2 + f * g.fsc, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twy);
+    }
+    rows_c2r(B.W2, (SR*)B.W1, (long long)nf * g.ny * g.nz);
+  }
+
+  // ---------------------------------------------------------------- fused passes
+  PassArgs args(const Geo& g, int stage, int store_rk, int cfl) {
+    PassArgs a;
+    a.g = g; a.P = P; a.hall = P.hall; a.aeb = P.aeb; a.stage = stage; a.store_rk = store_rk; a.cfl = cfl; a.st = st;
+    return a;
+  }
+  void passA(const PassArgs& a) { launch_passA<T>(stream, p.nz, B, a, pc, ktab(), twz); }
+  void passB(const PassArgs& a) { launch_passB<T>(stream, p.ny, B, a, pc, ktab(), twy); }
+  void passC(const PassArgs& a) { launch_passC<T>(stream, p.nx, B, a, pc, twx); }
+  void passD(const PassArgs& a) { launch_passD<T>(stream, p.ny, B, a, pc, ktab(), twy); }
+  void passE(const PassArgs& a) { launch_passE<T>(stream, p.nz, B, a, pc, ktab(), twz); }
+
+  // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage
+  const Geo& g_in() const { return (prune_ok && dealiased) ? gprune : gfull; }
+  const Geo& g_out() const { return prune_ok ? gprune : gfull; }
+
+  // one stage: stage = 0..2; cfl: compute the CFL minimum and finalise dt before D
+  void enqueue_stage(int stage, bool cfl, bool store_rk) {
+    const Geo& gi = g_in();
+    PassArgs ai = args(gi, stage, store_rk, cfl);
+    passA(ai);
+    passB(ai);
+    // pass C reads the inverse-side ranges and writes the forward-side kx range
+    PassArgs ac = ai;
+    ac.g.kx_keep = std::max(gi.kx_keep, g_out().kx_keep);
+    passC(ac);
+    if (cfl) {
+      k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl);
+      LAPS_CK(cudaGetLastError());
+    }
+    PassArgs ao = args(g_out(), stage, store_rk, 0);
+    // the first stage after an upload must also clear every mode outside the kept box
+    if (!dealiased) ao.g = gfull;
+    passD(ao);
+    passE(ao);
+    dealiased = true;
+  }
+  void enqueue_step() {
+    enqueue_stage(0, true, true);
+    enqueue_stage(1, false, true);
+    enqueue_stage(2, false, false);
+    k_advance_time<<<1, 32, 0, stream>>>(st, p.radius0, P.Ur);
+    LAPS_CK(cudaGetLastError());
+    tables();
+  }
+
+  void wait(int timeout_ms) override {
+    cudaEvent_t ev;
+    LAPS_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    LAPS_CK(cudaEventRecord(ev, stream));
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      cudaError_t e = cudaEventQuery(ev);
+      if (e == cudaSuccess) break;
+      if (e != cudaErrorNotReady) {
+        cudaEventDestroy(ev);
+        throw Error{LAPS_ECUDA, std::string("device error: ") + cudaGetErrorString(e)};
+      }
+      auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+      if (timeout_ms > 0 && ms > timeout_ms) {
+        cudaEventDestroy(ev);
+        throw Error{LAPS_ETIMEDOUT, "device work did not finish within the timeout"};
+      }
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    cudaEventDestroy(ev);
+  }
+  int tmo() const { return p.timeout_ms > 0 ? p.timeout_ms : 600000; }
+  void read_state() {
+    LAPS_CK(cudaMemcpyAsync(h_st, st, sizeof(StepState), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
+  }
+
+  // ---------------------------------------------------------------- API
+  void upload(const double* h, int layout) override {
+    const Geo& g = gfull;
+    double* stage = (double*)B.W2;  // 8 real float64 fields fit in 15 complex fields
+    LAPS_CK(cudaMemcpyAsync(stage, h, 8 * g.fsr * sizeof(double), cudaMemcpyHostToDevice, stream));
+    k_upload_convert<T><<<1024, 256, 0, stream>>>(stage, (SR*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma);
+    LAPS_CK(cudaGetLastError());
+    forward3d((const SR*)B.W1, B.U, 8);
+    // mhd.f90:135: dt = 0 before the first vardt, so the first CFL value is taken as is
+    LAPS_CK(cudaMemsetAsync(&st->dt, 0, sizeof(double), stream));
+    dealiased = false;
+    have_state = true;
+    wait(tmo());
+  }
+  void set_time(double t) override {
+    read_state();  // sync mirror
+    StepState s = *h_st;
+    s.time = t;
+    s.radius = p.radius0 + P.Ur * t;
+    s.inv_tau = P.Ur != 0.0 ? 1.0 / (s.radius / P.Ur) : 0.0;
+    s.r_ratio = p.radius0 / s.radius;
+    s.ksq_plain = 0;
+    LAPS_CK(cudaMemcpyAsync(st, &s, sizeof(s), cudaMemcpyHostToDevice, stream));
+    tables();
+    wait(tmo());
+  }
+  double vardt() override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    const Geo& gi = g_in();
+    PassArgs a = args(gi, 0, 0, 1);
+    passA(a);
+    passB(a);
+    PassArgs ac = a;
+    ac.cfl = 2;  // CFL only: skip the fluxes
+    passC(ac);
+    k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl);
+    LAPS_CK(cudaGetLastError());
+    read_state();
+    return h_st->dt;
+  }
+  void step(int n, double* time, double* dt, int* status) override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    LAPS_CK(cudaMemsetAsync(&st->status, 0, sizeof(int), stream));
+    LAPS_CK(cudaMemsetAsync(&st->halt, 0, sizeof(int), stream));
+    int done = 0;
+    if (!dealiased && n > 0) {  // first step after an upload runs unpruned, outside the graph
+      enqueue_step();
+      done = 1;
+    }
+    if (done < n) {
+      if (!graph_steady) {
+        cudaGraph_t gr;
+        LAPS_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step();
+        LAPS_CK(cudaStreamEndCapture(stream, &gr));
+        LAPS_CK(cudaGraphInstantiate(&graph_steady, gr, 0));
+        cudaGraphDestroy(gr);
+      }
+      for (; done < n; done++) LAPS_CK(cudaGraphLaunch(graph_steady, stream));
+    }
+    read_state();
+    if (time) *time = h_st->time;
+    if (dt) *dt = h_st->dt;
+    if (status) *status = h_st->status;
+  }
+  void rk_stage(int irk) override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    if (irk < 1 || irk > 3) throw Error{LAPS_EINVAL, "irk must be 1, 2 or 3"};
+    LAPS_CK(cudaMemsetAsync(&st->halt, 0, sizeof(int), stream));
+    enqueue_stage(irk - 1, false, true);
+    wait(tmo());
+  }
+  void download(double* uu, double* prim) override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    const Geo& g = gfull;
+    inverse3d(B.U, 8);
+    double* out = (double*)B.W2;  // 12 real float64 fields fit in 15 complex fields
+    k_download_convert<T><<<1024, 256, 0, stream>>>((const SR*)B.W1, uu ? out : nullptr, prim ? out + 8 * g.fsr : nullptr,
+                                                    g.fsr, P.gamma);
+    LAPS_CK(cudaGetLastError());
+    if (uu) LAPS_CK(cudaMemcpyAsync(uu, out, 8 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (prim) LAPS_CK(cudaMemcpyAsync(prim, out + 8 * g.fsr, 4 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
+  }
+  void download_spectral(double* uf) override {
+    const Geo& g = gfull;
+    double2* out = (double2*)B.W1;
+    k_spec_to_ref<T><<<1024, 256, 0, stream>>>(B.U, out, g, 8);
+    LAPS_CK(cudaGetLastError());
+    LAPS_CK(cudaMemcpyAsync(uf, out, (size_t)8 * g.nz * g.ny * g.nh * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
+  }
+  void upload_spectral(const double* uf) override {
+    const Geo& g = gfull;
+    double2* in = (double2*)B.W1;
+    LAPS_CK(cudaMemcpyAsync(in, uf, (size_t)8 * g.nz * g.ny * g.nh * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    k_spec_from_ref<T><<<1024, 256, 0, stream>>>(in, B.U, g, 8);
+    LAPS_CK(cudaGetLastError());
+    dealiased = false;
+    have_state = true;
+    wait(tmo());
+  }
+  void diagnostics(laps_diag* d) override;
+  void get_time(double* t, double* dt) override {
+    read_state();
+    if (t) *t = h_st->time;
+    if (dt) *dt = h_st->dt;
+  }
+  void info(laps_info* i) override {
+    i->device_bytes = bytes;
+    i->kx_keep = gprune.kx_keep;
+    i->ky_keep = gprune.nky();
+    i->kz_keep = gprune.nkz();
+    i->kernels_per_step = 3 * 5 + 3;
+    i->graph = graph_steady != nullptr;
+  }
+};
+
+// ---------------------------------------------------------------------------- diagnostics
+template <class T> void Engine<T>::diagnostics(laps_diag* d) {
+  if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+  const Geo& g = gfull;
+  read_state();
+  d->time = h_st->time;
+  d->dt = h_st->dt;
+  d->radius = h_st->radius;
+  inverse3d(B.U, 8);  // real conserved T fields in W1
+  int nb = npart;
+  // pass 1: sums of f and f^2 for the 8 reported fields, the energies and u.B
+  k_diag_sums<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, P.gamma, d_part);
+  LAPS_CK(cudaGetLastError());
+  std::vector<double> part((size_t)nb * 32);
+  LAPS_CK(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  wait(tmo());
+  double s[32] = {0};
+  for (int b = 0; b < nb; b++)
+    for (int k = 0; k < 19; k++) s[k] += part[(size_t)b * 32 + k];
+  double n = (double)g.fsr;
+  double ave[8];
+  for (int k = 0; k < 8; k++) {
+    ave[k] = s[k] / n;
+    d->uu_ave[k] = ave[k];
+    d->uu_rms[k] = s[8 + k] / n - ave[k] * ave[k];
+  }
+  d->e_kin = 0.5 * s[16] / n;
+  d->e_mag = 0.5 * s[17] / n;
+  d->h_cross = s[18] / n;
+  // pass 2: rho (u - <u>)^2
+  k_diag_rhou2<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, ave[1], ave[2], ave[3], d_part);
+  LAPS_CK(cudaGetLastError());
+  // spectral: max |ik.B| and <A.B>
+  k_diag_spec<T><<<nb, 256, 0, stream>>>(B.U, g, ktab(), P, pc, st, d_part + (size_t)nb * 8);
+  LAPS_CK(cudaGetLastError());
+  LAPS_CK(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  wait(tmo());
+  double r2[3] = {0, 0, 0}, hm = 0, mx = 0;
+  for (int b = 0; b < nb; b++) {
+    for (int k = 0; k < 3; k++) r2[k] += part[(size_t)b * 8 + k];
+    mx = std::fmax(mx, part[(size_t)nb * 8 + (size_t)b * 2 + 0]);
+    hm += part[(size_t)nb * 8 + (size_t)b * 2 + 1];
+  }
+  for (int k = 0; k < 3; k++) d->rho_u2[k] = r2[k] / n;
+  d->max_divB = mx;
+  d->h_mag = hm;
+}
+
+}  // namespace laps

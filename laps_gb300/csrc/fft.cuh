@@ -1,0 +1,188 @@
+// Batched 1-D complex FFTs of power-of-two length N held in shared memory.
+//
+// Algorithm: Stockham autosort (no bit reversal) with radix-16 stages and one final
+// radix-2/4/8 stage, each thread owning 16 elements of a line per stage (N >= 16;
+// a single radix-8 thread for N = 8).  For a stage of radix r after Ns points have been
+// combined, butterfly b (0 <= b < N/r) reads x[b + i N/r], multiplies by w^(i k N/(Ns r))
+// with k = b mod Ns, does an r-point DFT and writes y[(b / Ns) Ns r + k + i Ns].
+// This replaces the reference's per-line FFTW plans (src_compressible/fftw.f90:27-33),
+// which compute the same unnormalised DFT: sign -1 forward, +1 backward.
+//
+// Layout: element j of line `l` lives at s[j * JS + l * LS] (Store<T>::C units).  Column
+// tiles use JS = TX, LS = 1 (a quarter-warp touches one 128-byte row: conflict-free);
+// rows use JS = 1, LS = line pitch.
+#pragma once
+#include "arith.cuh"
+
+namespace laps {
+
+// compile-time float-float split of a double constant
+#define LAPS_KC(name, val)                         \
+  constexpr double name##_d = (val);              \
+  constexpr float name##_h = (float)(name##_d);   \
+  constexpr float name##_l = (float)(name##_d - (double)name##_h)
+
+template <class T> __device__ __forceinline__ T kc(double d, float h, float l);
+template <> __device__ __forceinline__ double kc<double>(double d, float, float) { return d; }
+template <> __device__ __forceinline__ dd kc<dd>(double, float h, float l) { return {h, l}; }
+template <> __device__ __forceinline__ float kc<float>(double, float h, float) { return h; }
+
+LAPS_KC(K_SQH, 0.70710678118654752440);   // sqrt(2)/2
+LAPS_KC(K_C8, 0.92387953251128675613);    // cos(pi/8)
+LAPS_KC(K_S8, 0.38268343236508977173);    // sin(pi/8)
+
+// x * exp(DIR * i * theta) for theta = pi/4 (w8), given cos = sin = sqrt(2)/2
+template <class T, int DIR> __device__ __forceinline__ cx<T> rot45(cx<T> x) {
+  const T c = kc<T>(K_SQH_d, K_SQH_h, K_SQH_l);
+  // DIR=-1: (1 - i)/sqrt2 * (a + ib) = ((a + b) + i (b - a)) / sqrt2
+  if (DIR < 0) return {(x.re + x.im) * c, (x.im - x.re) * c};
+  return {(x.re - x.im) * c, (x.im + x.re) * c};
+}
+template <class T, int DIR> __device__ __forceinline__ cx<T> rot135(cx<T> x) {
+  const T c = kc<T>(K_SQH_d, K_SQH_h, K_SQH_l);
+  // DIR=-1: (-1 - i)/sqrt2 * (a + ib) = ((b - a) + i (-a - b)) / sqrt2
+  if (DIR < 0) return {(x.im - x.re) * c, -((x.re + x.im) * c)};
+  return {-((x.re + x.im) * c), (x.re - x.im) * c};
+}
+// x * (c + DIR*i*s) with constants c, s
+template <class T, int DIR> __device__ __forceinline__ cx<T> rotcs(cx<T> x, T c, T s) {
+  if (DIR < 0) return {x.re * c + x.im * s, x.im * c - x.re * s};
+  return {x.re * c - x.im * s, x.im * c + x.re * s};
+}
+template <class T, int DIR> __device__ __forceinline__ cx<T> mul_dir_i(cx<T> x) {
+  return DIR < 0 ? times_mi(x) : times_i(x);
+}
+
+template <class T, int DIR> __device__ __forceinline__ void dft2(cx<T>* v) {
+  cx<T> a = v[0], b = v[1];
+  v[0] = a + b;
+  v[1] = a - b;
+}
+template <class T, int DIR> __device__ __forceinline__ void dft4(cx<T>& x0, cx<T>& x1, cx<T>& x2, cx<T>& x3) {
+  cx<T> a = x0 + x2, b = x0 - x2, c = x1 + x3, d = mul_dir_i<T, DIR>(x1 - x3);
+  x0 = a + c;
+  x2 = a - c;
+  x1 = b + d;
+  x3 = b - d;
+}
+template <class T, int DIR> __device__ __forceinline__ void dft4v(cx<T>* v) { dft4<T, DIR>(v[0], v[1], v[2], v[3]); }
+template <class T, int DIR> __device__ __forceinline__ void dft8(cx<T>* v) {
+  // decimation in time: E = DFT4(x0,x2,x4,x6), O = DFT4(x1,x3,x5,x7)
+  cx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  cx<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<T, DIR>(e0, e1, e2, e3);
+  dft4<T, DIR>(o0, o1, o2, o3);
+  o1 = rot45<T, DIR>(o1);
+  o2 = mul_dir_i<T, DIR>(o2);
+  o3 = rot135<T, DIR>(o3);
+  v[0] = e0 + o0; v[4] = e0 - o0;
+  v[1] = e1 + o1; v[5] = e1 - o1;
+  v[2] = e2 + o2; v[6] = e2 - o2;
+  v[3] = e3 + o3; v[7] = e3 - o3;
+}
+template <class T, int DIR> __device__ __forceinline__ void dft16(cx<T>* v) {
+  // four-step 4 x 4: n = n1 + 4 n2, k = k2 + 4 k1
+  cx<T> y[16];
+#pragma unroll
+  for (int n1 = 0; n1 < 4; n1++) {
+    cx<T> a = v[n1], b = v[n1 + 4], c = v[n1 + 8], d = v[n1 + 12];
+    dft4<T, DIR>(a, b, c, d);
+    y[n1 * 4 + 0] = a; y[n1 * 4 + 1] = b; y[n1 * 4 + 2] = c; y[n1 * 4 + 3] = d;
+  }
+  const T c8 = kc<T>(K_C8_d, K_C8_h, K_C8_l), s8 = kc<T>(K_S8_d, K_S8_h, K_S8_l);
+  // twiddles w16^(n1 k2)
+  y[1 * 4 + 1] = rotcs<T, DIR>(y[5], c8, s8);          // w^1
+  y[1 * 4 + 2] = rot45<T, DIR>(y[6]);                  // w^2
+  y[1 * 4 + 3] = rotcs<T, DIR>(y[7], s8, c8);          // w^3
+  y[2 * 4 + 1] = rot45<T, DIR>(y[9]);                  // w^2
+  y[2 * 4 + 2] = mul_dir_i<T, DIR>(y[10]);             // w^4
+  y[2 * 4 + 3] = rot135<T, DIR>(y[11]);                // w^6
+  y[3 * 4 + 1] = rotcs<T, DIR>(y[13], s8, c8);         // w^3
+  y[3 * 4 + 2] = rot135<T, DIR>(y[14]);                // w^6
+  y[3 * 4 + 3] = -rotcs<T, DIR>(y[15], c8, s8);       // w^9 = -w^1
+#pragma unroll
+  for (int k2 = 0; k2 < 4; k2++) {
+    cx<T> a = y[0 * 4 + k2], b = y[1 * 4 + k2], c = y[2 * 4 + k2], d = y[3 * 4 + k2];
+    dft4<T, DIR>(a, b, c, d);
+    v[k2] = a; v[k2 + 4] = b; v[k2 + 8] = c; v[k2 + 12] = d;
+  }
+}
+template <class T, int DIR, int R> __device__ __forceinline__ void dft_r(cx<T>* v) {
+  if (R == 2) dft2<T, DIR>(v);
+  else if (R == 4) dft4v<T, DIR>(v);
+  else if (R == 8) dft8<T, DIR>(v);
+  else dft16<T, DIR>(v);
+}
+
+// Stage plan for length N.
+template <int N> struct Plan {
+  static constexpr int EPT = N >= 16 ? 16 : N;               // elements per thread per stage
+  static constexpr int TPL = N / EPT;                        // threads per line
+  static constexpr int NS16 = N >= 16 ? (N >= 4096 ? 3 : N >= 256 ? 2 : 1) : 0;
+  static constexpr int REST = N >= 16 ? N / (NS16 == 1 ? 16 : NS16 == 2 ? 256 : 4096) : N;
+  static constexpr int NSTAGE = NS16 + (REST > 1 ? 1 : 0);
+};
+
+// twiddle w_N^m (DIR=-1: exp(-2 pi i m/N)), read from a table of exp(-2 pi i j/Ntab)
+template <class T, int DIR>
+__device__ __forceinline__ cx<T> twiddle(const typename Store<T>::C* __restrict__ tw, int idx) {
+  cx<T> w = Store<T>::ldg(tw + idx);
+  return DIR < 0 ? w : conj(w);
+}
+
+// One Stockham stage of radix R after NS points have been combined, for every line of the
+// tile.  Thread t of line l; threads with active == false only join the two barriers.
+template <class T, int N, int DIR, int R, int NS, int JS, int LS>
+__device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t, bool active,
+                                          const typename Store<T>::C* __restrict__ tw, int twstep) {
+  using P = Plan<N>;
+  constexpr int NB = P::EPT / R;  // butterflies per thread
+  cx<T> v[NB][R];
+  typename Store<T>::C* line = s + l * LS;
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < NB; q++) {
+      int b = t + q * P::TPL;
+#pragma unroll
+      for (int i = 0; i < R; i++) v[q][i] = Store<T>::ldc(line + (b + i * (N / R)) * JS);
+      if (NS > 1) {
+        int k = b % NS;
+        int step = k * (N / (NS * R)) * twstep;
+#pragma unroll
+        for (int i = 1; i < R; i++) v[q][i] = v[q][i] * twiddle<T, DIR>(tw, i * step);
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < NB; q++) {
+      int b = t + q * P::TPL;
+      int k = b % NS;
+      dft_r<T, DIR, R>(v[q]);
+      int base = (b / NS) * NS * R + k;
+#pragma unroll
+      for (int i = 0; i < R; i++) Store<T>::stc(line + (base + i * NS) * JS, v[q][i]);
+    }
+  }
+  __syncthreads();
+}
+
+// Full FFT of every line of the tile (unnormalised).  Every thread of the block calls it.
+// tw: table of exp(-2 pi i j / (N*twstep)), j = 0..N*twstep-1.
+template <class T, int N, int DIR, int JS, int LS>
+__device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t, bool active,
+                                          const typename Store<T>::C* __restrict__ tw, int twstep) {
+  using P = Plan<N>;
+  if constexpr (N < 16) {
+    fft_stage<T, N, DIR, N, 1, JS, LS>(s, l, t, active, tw, twstep);
+  } else {
+    fft_stage<T, N, DIR, 16, 1, JS, LS>(s, l, t, active, tw, twstep);
+    if constexpr (P::NS16 >= 2) fft_stage<T, N, DIR, 16, 16, JS, LS>(s, l, t, active, tw, twstep);
+    if constexpr (P::NS16 >= 3) fft_stage<T, N, DIR, 16, 256, JS, LS>(s, l, t, active, tw, twstep);
+    constexpr int NSR = P::NS16 == 1 ? 16 : P::NS16 == 2 ? 256 : 4096;
+    if constexpr (P::REST > 1) fft_stage<T, N, DIR, P::REST, NSR, JS, LS>(s, l, t, active, tw, twstep);
+  }
+}
+
+}  // namespace laps

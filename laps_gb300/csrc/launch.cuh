@@ -1,0 +1,46 @@
+// Kernel launchers, one switch over the supported line lengths per pass.  Each launcher
+// is explicitly instantiated per element type in its own translation unit (launch_*.cu)
+// so that the float-float FFT code compiles in parallel.
+#pragma once
+#include <string>
+#include "passes.cuh"
+
+namespace laps {
+
+inline int ilog2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define LAPS_CK(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) throw Error{LAPS_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+#define LAPS_COL_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512)
+#define LAPS_ROW_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512)
+
+template <class K> inline void set_smem(K kernel, int bytes) {
+  if (bytes > 48 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+
+template <class T>
+void launch_col_plain(cudaStream_t stream, const typename Store<T>::C* in, typename Store<T>::C* out, long long fs, int nf, int N,
+                      int dir, int jstride, int ostride, int ncol, int nouter, int sexp, const typename Store<T>::C* tw);
+template <class T>
+void launch_rows_r2c(cudaStream_t stream, int nx, const typename Store<T>::R* in, typename Store<T>::C* out, long long nrows, int kxp,
+                     const typename Store<T>::C* twx);
+template <class T>
+void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in, typename Store<T>::R* out, long long nrows, int kxp,
+                     const typename Store<T>::C* twx);
+template <class T> void launch_passA(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+template <class T> void launch_passB(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+template <class T> void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw);
+template <class T> void launch_passD(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+template <class T> void launch_passE(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+
+}  // namespace laps

@@ -1,0 +1,122 @@
+// Definitions of the kernel launchers declared in launch.cuh.
+#pragma once
+#include "launch.cuh"
+
+namespace laps {
+
+template <class T>
+void launch_col_plain(cudaStream_t stream, const typename Store<T>::C* in, typename Store<T>::C* out, long long fs, int nf, int N,
+                      int dir, int jstride, int ostride, int ncol, int nouter, int sexp, const typename Store<T>::C* tw) {
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    dim3 grid((ncol + TX - 1) / TX, (nouter + CL::NTILE - 1) / CL::NTILE, nf);                                          \
+    if (dir < 0) {                                                                                                      \
+      set_smem(k_col_plain<T, NN, -1>, CL::SMEM);                                                                       \
+      k_col_plain<T, NN, -1><<<grid, CL::THREADS, CL::SMEM, stream>>>(in, out, fs, jstride, ostride, ncol, nouter, sexp, tw); \
+    } else {                                                                                                            \
+      set_smem(k_col_plain<T, NN, 1>, CL::SMEM);                                                                        \
+      k_col_plain<T, NN, 1><<<grid, CL::THREADS, CL::SMEM, stream>>>(in, out, fs, jstride, ostride, ncol, nouter, sexp, tw); \
+    }                                                                                                                   \
+    break;                                                                                                              \
+  }
+  switch (N) { LAPS_COL_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported column length"}; }
+#undef LAPS_CASE
+  LAPS_CK(cudaGetLastError());
+}
+
+template <class T>
+void launch_rows_r2c(cudaStream_t stream, int nx, const typename Store<T>::R* in, typename Store<T>::C* out, long long nrows, int kxp,
+                     const typename Store<T>::C* twx) {
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    int sm = RowP<NN>::LB * NN * (int)sizeof(typename Store<T>::R);                                                     \
+    set_smem(k_row_r2c<T, NN>, sm);                                                                                     \
+    k_row_r2c<T, NN><<<(unsigned)((nrows + RowP<NN>::LB - 1) / RowP<NN>::LB), 128, sm, stream>>>(in, out, nrows, kxp, -ilog2(NN), twx); \
+    break;                                                                                                              \
+  }
+  switch (nx) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }
+#undef LAPS_CASE
+  LAPS_CK(cudaGetLastError());
+}
+
+template <class T>
+void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in, typename Store<T>::R* out, long long nrows, int kxp,
+                     const typename Store<T>::C* twx) {
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    int sm = RowP<NN>::LB * NN * (int)sizeof(typename Store<T>::R);                                                     \
+    set_smem(k_row_c2r<T, NN>, sm);                                                                                     \
+    k_row_c2r<T, NN><<<(unsigned)((nrows + RowP<NN>::LB - 1) / RowP<NN>::LB), 128, sm, stream>>>(in, out, nrows, kxp, twx); \
+    break;                                                                                                              \
+  }
+  switch (nx) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }
+#undef LAPS_CASE
+  LAPS_CK(cudaGetLastError());
+}
+
+#define LAPS_COL_PASS(NAME, KERNEL, NOUTER)                                                                              \
+  template <class T>                                                                                                    \
+  void NAME(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw) {    \
+    switch (N) { LAPS_COL_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported line length"}; }               \
+    LAPS_CK(cudaGetLastError());                                                                                        \
+  }
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    set_smem(k_passA<T, NN>, CL::SMEM);                                                                                 \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE);                                    \
+    k_passA<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    break;                                                                                                              \
+  }
+LAPS_COL_PASS(launch_passA, k_passA, nky)
+#undef LAPS_CASE
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    set_smem(k_passB<T, NN>, CL::SMEM);                                                                                 \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE);                                       \
+    k_passB<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    break;                                                                                                              \
+  }
+LAPS_COL_PASS(launch_passB, k_passB, nz)
+#undef LAPS_CASE
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    set_smem(k_passD<T, NN>, CL::SMEM);                                                                                 \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE);                                       \
+    k_passD<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    break;                                                                                                              \
+  }
+LAPS_COL_PASS(launch_passD, k_passD, nz)
+#undef LAPS_CASE
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    set_smem(k_passE<T, NN>, CL::SMEM);                                                                                 \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE);                                    \
+    k_passE<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    break;                                                                                                              \
+  }
+LAPS_COL_PASS(launch_passE, k_passE, nky)
+#undef LAPS_CASE
+#undef LAPS_COL_PASS
+
+template <class T>
+void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CF = PassCCfg<NN>;                                                                                            \
+    int sm = CF::ROWS * CF::NF * NN * (int)sizeof(typename Store<T>::R);                                                \
+    set_smem(k_passC<T, NN>, sm);                                                                                       \
+    long long rows = (long long)a.g.ny * a.g.nz;                                                                        \
+    k_passC<T, NN><<<(unsigned)(rows / CF::ROWS), 128, sm, stream>>>(B, a, pc, tw);                                     \
+    break;                                                                                                              \
+  }
+  switch (N) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }
+#undef LAPS_CASE
+  LAPS_CK(cudaGetLastError());
+}
+
+}  // namespace laps

@@ -1,0 +1,5 @@
+// Pass B launcher (dd).
+#include "launch_defs.cuh"
+namespace laps {
+template void launch_passB<dd>(cudaStream_t, int, Bufs<dd>, PassArgs, PT<dd>, KTab<dd>, const Store<dd>::C*);
+}  // namespace laps

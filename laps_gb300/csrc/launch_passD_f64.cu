@@ -1,0 +1,5 @@
+// Pass D launcher (double).
+#include "launch_defs.cuh"
+namespace laps {
+template void launch_passD<double>(cudaStream_t, int, Bufs<double>, PassArgs, PT<double>, KTab<double>, const Store<double>::C*);
+}  // namespace laps

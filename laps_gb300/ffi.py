@@ -1,0 +1,216 @@
+"""ctypes binding of ``include/laps_gpu.h`` (the C-ABI of ``liblaps_gpu.so``).
+
+This is the Python host's view of the drop-in boundary: the same entry points a Fortran
+host binds through ``iso_c_binding`` (``fortran/laps_gpu.f90``).  Arrays cross as float64
+in the reference's Fortran order ``uu(ix,iy,iz,ivar)``, i.e. numpy ``[ivar, iz, iy, ix]``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "liblaps_gpu.so"
+HEADER = PKG.parent / "include" / "laps_gpu.h"
+
+LAPS_OK = 0
+LAPS_EINVAL = -1
+LAPS_ENOMEM = -2
+LAPS_ECUDA = -3
+LAPS_ETIMEDOUT = -4
+LAPS_ESTATE = -5
+LAPS_STATUS_NAN = 1
+LAPS_STATUS_DT_FLOOR = 2
+VARIANT_3DC, VARIANT_3DI, VARIANT_2DC = 0, 1, 2
+PREC_FP64, PREC_DD, PREC_FP32 = 0, 1, 2
+LAYOUT_PRIMITIVE, LAYOUT_CONSERVED = 0, 1
+
+
+class laps_params(C.Structure):
+    _fields_ = [
+        ("variant", C.c_int), ("precision", C.c_int),
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("Lx", C.c_double), ("Ly", C.c_double), ("Lz", C.c_double),
+        ("adiabatic_index", C.c_double),
+        ("if_resis", C.c_int), ("if_resis_exp", C.c_int), ("resistivity", C.c_double),
+        ("if_visc", C.c_int), ("if_visc_exp", C.c_int), ("viscosity", C.c_double),
+        ("if_conserve_background", C.c_int),
+        ("dealias_option", C.c_int), ("afx", C.c_double), ("afy", C.c_double), ("afz", C.c_double),
+        ("cfl", C.c_double),
+        ("if_AEB", C.c_int), ("radius0", C.c_double), ("Ur0", C.c_double),
+        ("if_corotating", C.c_int), ("corotating_angle", C.c_double),
+        ("if_Hall", C.c_int), ("ion_inertial_length", C.c_double),
+        ("device", C.c_int), ("timeout_ms", C.c_int), ("mem_cap_bytes", C.c_longlong),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+class laps_diag(C.Structure):
+    _fields_ = [
+        ("time", C.c_double), ("dt", C.c_double), ("radius", C.c_double),
+        ("uu_ave", C.c_double * 8), ("uu_rms", C.c_double * 8), ("rho_u2", C.c_double * 3),
+        ("max_divB", C.c_double), ("e_kin", C.c_double), ("e_mag", C.c_double),
+        ("h_cross", C.c_double), ("h_mag", C.c_double),
+    ]
+
+
+class laps_info(C.Structure):
+    _fields_ = [
+        ("device_bytes", C.c_longlong), ("kx_keep", C.c_int), ("ky_keep", C.c_int), ("kz_keep", C.c_int),
+        ("kernels_per_step", C.c_int), ("graph", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load ``liblaps_gpu.so`` (building it first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        from . import build as _b
+        _b.build()
+    lib = C.CDLL(str(p))
+    P = C.POINTER
+    vp = C.c_void_p
+    dp = P(C.c_double)
+    sig = {
+        "laps_params_default": (C.c_int, [P(laps_params)]),
+        "laps_create": (C.c_int, [P(laps_params), P(vp)]),
+        "laps_destroy": (None, [vp]),
+        "laps_upload_state": (C.c_int, [vp, dp, C.c_int]),
+        "laps_set_time": (C.c_int, [vp, C.c_double]),
+        "laps_vardt": (C.c_int, [vp, dp]),
+        "laps_step": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
+        "laps_rk_stage": (C.c_int, [vp, C.c_int]),
+        "laps_download_state": (C.c_int, [vp, dp, dp]),
+        "laps_download_spectral": (C.c_int, [vp, dp]),
+        "laps_upload_spectral": (C.c_int, [vp, dp]),
+        "laps_diagnostics": (C.c_int, [vp, P(laps_diag)]),
+        "laps_wait": (C.c_int, [vp, C.c_int]),
+        "laps_get_time": (C.c_int, [vp, dp, dp]),
+        "laps_get_info": (C.c_int, [vp, P(laps_info)]),
+        "laps_last_error": (C.c_char_p, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class LapsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"laps error {code}: {msg}")
+        self.code = code
+
+
+def params(**kw) -> laps_params:
+    """Reference defaults (``laps_params_default``) overridden by keyword arguments."""
+    lib = load()
+    p = laps_params()
+    lib.laps_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Laps:
+    """One GPU run: the reference's hot-path subroutines as methods over a context."""
+
+    def __init__(self, p: laps_params):
+        self.lib = load()
+        self.p = p
+        h = C.c_void_p()
+        rc = self.lib.laps_create(C.byref(p), C.byref(h))
+        if rc != LAPS_OK:
+            raise LapsError(rc, self.lib.laps_last_error(None).decode())
+        self.h = h
+        self.shape = (p.nz, p.ny, p.nx)
+
+    def _ck(self, rc):
+        if rc != LAPS_OK:
+            raise LapsError(rc, self.lib.laps_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.laps_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- reference routines
+    def upload_state(self, uu: np.ndarray, primitive: bool = True):
+        a = np.ascontiguousarray(uu, dtype=np.float64)
+        assert a.shape == (8,) + self.shape
+        self._ck(self.lib.laps_upload_state(self.h, _dptr(a), LAYOUT_PRIMITIVE if primitive else LAYOUT_CONSERVED))
+
+    def set_time(self, t: float):
+        self._ck(self.lib.laps_set_time(self.h, float(t)))
+
+    def vardt(self) -> float:
+        d = C.c_double()
+        self._ck(self.lib.laps_vardt(self.h, C.byref(d)))
+        return d.value
+
+    def step(self, n: int = 1):
+        t, d, s = C.c_double(), C.c_double(), C.c_int()
+        self._ck(self.lib.laps_step(self.h, int(n), C.byref(t), C.byref(d), C.byref(s)))
+        return t.value, d.value, s.value
+
+    def rk_stage(self, irk: int):
+        self._ck(self.lib.laps_rk_stage(self.h, int(irk)))
+
+    def download_state(self):
+        uu = np.empty((8,) + self.shape)
+        prim = np.empty((4,) + self.shape)
+        self._ck(self.lib.laps_download_state(self.h, _dptr(uu), _dptr(prim)))
+        return uu, prim
+
+    def download_spectral(self):
+        nz, ny, nx = self.shape
+        uf = np.empty((8, nz, ny, nx // 2 + 1), np.complex128)
+        self._ck(self.lib.laps_download_spectral(self.h, uf.ctypes.data_as(C.POINTER(C.c_double))))
+        return uf
+
+    def upload_spectral(self, uf: np.ndarray):
+        a = np.ascontiguousarray(uf, dtype=np.complex128)
+        self._ck(self.lib.laps_upload_spectral(self.h, a.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def diagnostics(self) -> laps_diag:
+        d = laps_diag()
+        self._ck(self.lib.laps_diagnostics(self.h, C.byref(d)))
+        return d
+
+    def time(self):
+        t, d = C.c_double(), C.c_double()
+        self._ck(self.lib.laps_get_time(self.h, C.byref(t), C.byref(d)))
+        return t.value, d.value
+
+    def info(self) -> laps_info:
+        i = laps_info()
+        self._ck(self.lib.laps_get_info(self.h, C.byref(i)))
+        return i
+
+    def wait(self, timeout_ms: int = 600000):
+        self._ck(self.lib.laps_wait(self.h, int(timeout_ms)))

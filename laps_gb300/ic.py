@@ -1,0 +1,99 @@
+"""Seeded initial conditions in the reference's primitive layout.
+
+The arrays returned here are what LAPS reads back from ``outNNN.dat`` through its restart
+path (``src_compressible/restart.f90:17-63``): primitive variables
+``(rho, ux, uy, uz, Bx, By, Bz, p)`` in Fortran order ``(nx, ny, nz, 8)``, stored in numpy
+as ``[ivar, iz, iy, ix]``.  The conserved form is formed afterwards by
+``initial_calc_conserve_variable`` (``src_compressible/mhdinit.f90:1038-1056``), on the GPU
+by ``laps_upload_state``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+PI = 3.141592653589793
+
+
+def random_phase_spectrum(shape, L, kmin, kmax, alpha, rng):
+    """One divergence-free random vector field with |k|^alpha amplitudes on kmin <= |k| <= kmax.
+
+    Integer wave vectors (in units of 2 pi / L) inside the shell get an independent complex
+    Gaussian direction with a uniform random phase and amplitude |k|^alpha, are projected
+    onto the plane perpendicular to k, and are transformed to real space (the half
+    spectrum's implied Hermitian partner makes the field real).  Returns ``[3, nz, ny, nx]``
+    with zero mean and unit rms of |v|.
+    """
+    nz, ny, nx = shape
+    Lx, Ly, Lz = L
+    mx = np.arange(nx // 2 + 1)
+    my = np.fft.fftfreq(ny, 1.0 / ny)
+    mz = np.fft.fftfreq(nz, 1.0 / nz)
+    KZ, KY, KX = np.meshgrid(mz * (2 * PI / Lz), my * (2 * PI / Ly), mx * (2 * PI / Lx), indexing="ij")
+    MZ, MY, MX = np.meshgrid(mz, my, mx, indexing="ij")
+    kmag = np.sqrt(MX**2 + MY**2 + MZ**2)
+    shell = (kmag >= kmin) & (kmag <= kmax)
+    amp = np.where(shell, np.power(np.where(shell, kmag, 1.0), alpha), 0.0)
+    v = rng.standard_normal((3,) + kmag.shape) + 1j * rng.standard_normal((3,) + kmag.shape)
+    phase = np.exp(2j * PI * rng.random(kmag.shape))
+    v = v * (amp * phase)[None]
+    k2 = KX**2 + KY**2 + KZ**2
+    k2s = np.where(k2 > 0, k2, 1.0)
+    kdotv = (KX * v[0] + KY * v[1] + KZ * v[2]) / k2s
+    v[0] -= kdotv * KX
+    v[1] -= kdotv * KY
+    v[2] -= kdotv * KZ
+    out = np.fft.irfftn(v, s=(nz, ny, nx), axes=(1, 2, 3))
+    out -= out.mean(axis=(1, 2, 3), keepdims=True)
+    rms = math.sqrt(float(np.mean(np.sum(out**2, axis=0))))
+    if rms > 0:
+        out /= rms
+    return out
+
+
+def turbulence_ic(n, L=2 * PI, kmin=1, kmax=4, alpha=-1.0, rms_u=0.3, rms_b=0.3, seed=0,
+                  rho0=1.0, p0=0.1, B0=(1.0, 0.0, 0.0)):
+    """Uniform background plus random-phase divergence-free du, db (u drawn first, then b).
+
+    ``n`` is an int (cube) or an ``(nx, ny, nz)`` triple; returns ``[8, nz, ny, nx]`` float64.
+    """
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
+    Ls = (L, L, L) if np.isscalar(L) else tuple(L)
+    rng = np.random.default_rng(seed)
+    du = random_phase_spectrum((nz, ny, nx), Ls, kmin, kmax, alpha, rng) * rms_u
+    db = random_phase_spectrum((nz, ny, nx), Ls, kmin, kmax, alpha, rng) * rms_b
+    prim = np.empty((8, nz, ny, nx))
+    prim[0] = rho0
+    prim[1:4] = du
+    prim[4] = B0[0] + db[0]
+    prim[5] = B0[1] + db[1]
+    prim[6] = B0[2] + db[2]
+    prim[7] = p0
+    return prim
+
+
+def alfven_wave_ic(n, L=2 * PI, rho0=1.0, p0=0.1, bx0=1.0, db0=0.1, mode=1, cor_angle=0.0):
+    """Circularly polarised Alfven wave (``ipert=1`` over ``ifield=3``).
+
+    ``src_compressible/mhdinit.f90:246-251`` (uniform background) and ``:328-342``
+    (the wave); an exact nonlinear solution that travels along +x at v_A = bx0/sqrt(rho0).
+    """
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
+    Lx = L if np.isscalar(L) else L[0]
+    x = np.arange(nx) * (Lx / nx)
+    kx = 2 * PI / Lx * mode
+    s, c = np.sin(kx * x), np.cos(kx * x)
+    sa, ca = math.sin(cor_angle), math.cos(cor_angle)
+    prim = np.zeros((8, nz, ny, nx))
+    prim[0] = rho0
+    prim[4] = bx0
+    prim[7] = p0
+    sr = math.sqrt(rho0)
+    prim[6] = prim[6] - db0 * s
+    prim[3] = prim[3] + db0 / sr * s
+    prim[1] = prim[1] + db0 / sr * c * sa
+    prim[4] = prim[4] - db0 * c * sa
+    prim[2] = prim[2] + db0 / sr * c * ca
+    prim[5] = prim[5] - db0 * c * ca
+    return prim

@@ -1,0 +1,77 @@
+"""CPU checks of the C-ABI boundary: the library loads, exports every entry point the
+header declares, its structs have the C layout, and argument validation fails with the
+documented codes before any device call."""
+import ctypes
+import re
+import subprocess
+import tempfile
+from pathlib import Path
+
+import pytest
+
+from laps_gb300 import ffi
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_functions():
+    txt = (ROOT / "include" / "laps_gpu.h").read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(laps_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = header_functions()
+    assert len(names) >= 16
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layout_matches_c(tmp_path):
+    src = tmp_path / "sz.c"
+    fields = [f[0] for f in ffi.laps_params._fields_]
+    body = "\n".join(f'printf("%zu ", offsetof(laps_params, {f}));' for f in fields)
+    src.write_text(
+        "#include <stdio.h>\n#include <stddef.h>\n#include \"laps_gpu.h\"\nint main(){"
+        + body
+        + 'printf("%zu %zu %zu\\n", sizeof(laps_params), sizeof(laps_diag), sizeof(laps_info));return 0;}'
+    )
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    offs = [getattr(ffi.laps_params, f).offset for f in fields]
+    assert [int(x) for x in out[: len(fields)]] == offs
+    assert int(out[-3]) == ctypes.sizeof(ffi.laps_params)
+    assert int(out[-2]) == ctypes.sizeof(ffi.laps_diag)
+    assert int(out[-1]) == ctypes.sizeof(ffi.laps_info)
+
+
+def test_defaults_are_reference_initialisers(lib):
+    p = ffi.params()
+    assert (p.nx, p.ny, p.nz) == (128, 128, 64)  # mhdinit.f90:5
+    assert p.dealias_option == 2 and p.afx == 0.495  # dealiasing.f90:11-12
+    assert p.cfl == 0.5 and p.radius0 == 30.0
+    assert abs(p.adiabatic_index - 5.0 / 3.0) < 1e-15
+
+
+@pytest.mark.parametrize(
+    "kw,code",
+    [
+        (dict(nx=100), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=48, nz=64), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, precision=7), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, variant=1), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, cfl=0.0), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, mem_cap_bytes=1 << 20), ffi.LAPS_ENOMEM),
+    ],
+)
+def test_create_rejects_bad_parameters(lib, kw, code):
+    with pytest.raises(ffi.LapsError) as e:
+        ffi.Laps(ffi.params(**kw))
+    assert e.value.code == code
+    assert lib.laps_last_error(None)
+
+
+def test_null_context_is_an_error(lib):
+    assert lib.laps_step(None, 1, None, None, None) == ffi.LAPS_EINVAL
+    assert lib.laps_wait(None, 10) == ffi.LAPS_EINVAL
