@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""Throughput of the LAPS RHS + RK3 step on GB300: grid-point-steps per second.
+
+Workload: the 3-D compressible Hall-MHD run with the expanding box at 256^3 (d_i = 0.05,
+Ur0/R0 = 0.01, eta = nu = 5e-4, 2/3 mask, cfl 0.4, random-phase 1 <= |k| <= 8 spectrum with
+rms 0.5, seed 1), seeded synthetic initial condition.  A "step" is one full time step
+(CFL, three RK stages, radius update) of the whole grid.
+
+Our arm (default): the float-float engine through the C-ABI.  `value` is device-timed with
+CUDA events on the engine's stream, state resident in HBM; `e2e` is the same metric through
+the C-ABI with host buffers (pinned upload of the primitive initial state, one laps_step call
+per step returning time/dt/status to the host, download of the final state).
+
+--impl reference: the reference's CPU algorithm (the oracle restatement, pocketfft with all
+host threads) timed on a bounded sample of the same workload.
+
+For N > 1 (torchrun) every rank advances its own independent replica ("replicas only":
+one run does not shard); value = all ranks' grid-point-steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "grid-point-steps/s vs plain FP64 at stated spectrum error; FFT HBM GB/s % peak"
+N_GRID = 256
+WORKLOAD = "3D compressible Hall-MHD + expanding box, 256^3"
+CFG2 = dict(if_resis=1, resistivity=5e-4, if_visc=1, viscosity=5e-4, dealias_option=1, cfl=0.4,
+            if_Hall=1, ion_inertial_length=0.05, if_AEB=1, radius0=30.0, Ur0=0.3)
+PASS_NAMES = ["A_inv_z", "B_inv_y", "C_x_flux", "D_fwd_y", "E_fwd_z_rk", "bookkeeping"]
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value: float, ws: int):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def initial_state(n=N_GRID):
+    from laps_gb300.ic import turbulence_ic
+
+    return turbulence_ic(n, kmin=1, kmax=8, alpha=-1.0, rms_u=0.5, rms_b=0.5, seed=1)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# algorithmic HBM bytes of one launch of each pass (compulsory reads + writes of the
+# dataflow implemented): S_* are element counts of the touched sub-boxes
+def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, elem=16):
+    kxp8 = int(math.ceil(kx_keep / 8.0) * 8)
+    col_A = kxp8 * nky            # columns of pass A / E
+    col_B = kxp8 * n              # columns of pass B / D (one per z plane)
+    nin = 8 + (3 if hall else 0)
+    nfl = 18 + (1 if aeb else 0)
+    A = elem * col_A * (8 * nkz + (10 if hall else 8) * n)
+    B = elem * col_B * ((10 if hall else 8) * nky + nin * n)
+    C = elem * n * n * kx_keep * (nin + nfl)
+    D = elem * col_B * (nfl * n + 15 * nky)
+    E = elem * col_A * (15 * n + 8 * nkz * 4)  # read 15 columns; read U, R and write U, R on kept kz
+    return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
+
+
+def cpu_sample(steps, warmup, n=N_GRID):
+    """The oracle restatement of the reference's step on the host cores: warmup + timed steps
+    at the full grid.  Returns (grid-point-steps/s, threads, sample text)."""
+    from oracle import laps3d
+
+    o = laps3d.restart(n, CFG2, initial_state(n))
+    for _ in range(warmup):
+        o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    el = time.perf_counter() - t0
+    return n**3 * steps / el, laps3d._WORKERS, f"{warmup} warm-up + {steps} timed steps at {n}^3 (numpy + scipy.fft pocketfft)"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    k = max(1, min(args.steps, args.ref_steps))
+    w = min(args.warmup, 1)
+    v, cores, sample = cpu_sample(k, w)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-point-steps/s", "n_gpus": args.gpus,
+        "steps": k, "warmup": w, "ms_per_step": N_GRID**3 / v * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-phase spectrum)",
+        "config": {"workload": WORKLOAD, "grid": N_GRID, "variant": "3DC", "hall": 0.05, "expanding_box": "Ur0/R0=0.01",
+                   "dealias": "2/3 sphere", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    from laps_gb300 import ffi
+
+    prec = {"dd": ffi.PREC_DD, "fp64": ffi.PREC_FP64}[args.precision]
+    n = N_GRID
+    prim = initial_state(n)
+    p = ffi.params(nx=n, ny=n, nz=n, precision=prec, device=local, **CFG2)
+    g = ffi.Laps(p)
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    g.step(max(args.warmup, 3) if args.warmup >= 3 else args.warmup)
+    info = g.info()
+    # ---- device-resident timed region: K steps, CUDA events around every pass
+    barrier(ws)
+    with Clocks(local) as clk:
+        pass_ms, total_ms, status = g.step_profiled(args.steps)
+    barrier(ws)
+    tmax = barrier_max(total_ms, ws)
+    value = ws * n**3 * args.steps / (tmax * 1e-3)
+    # ---- graph path, same state continues (reported beside)
+    t0 = time.perf_counter()
+    g.step(args.steps)
+    graph_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # ---- end to end through the C-ABI with host buffers
+    import ctypes
+
+    lib = ffi.load()
+    host_in = np.ascontiguousarray(prim)
+    host_out = np.empty((8,) + prim.shape[1:])
+    host_prim = np.empty((4,) + prim.shape[1:])
+    try:  # pin the host buffers (cudaHostRegister) so the copies run at link speed
+        import torch
+
+        torch.cuda.set_device(local)
+        for a in (host_in, host_out, host_prim):
+            torch.cuda.cudart().cudaHostRegister(a.ctypes.data, a.nbytes, 0)
+        pinned = True
+    except Exception:
+        pinned = False
+    e2e_ctx = ffi.Laps(p)
+    e2e_ctx.upload_state(host_in, primitive=True)  # warm the path once
+    e2e_ctx.set_time(0.0)
+    e2e_ctx.step(2)
+    barrier(ws)
+    t0 = time.perf_counter()
+    e2e_ctx.upload_state(host_in, primitive=True)
+    e2e_ctx.set_time(0.0)
+    for _ in range(args.steps):
+        e2e_ctx.step(1)  # returns time, dt, status to the host every step
+    rc = lib.laps_download_state(e2e_ctx.h, host_out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                 host_prim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == 0
+    e2e_s = barrier_max(time.perf_counter() - t0, ws)
+    e2e_v = ws * n**3 * args.steps / e2e_s
+    h2d = host_in.nbytes / args.steps + 16
+    d2h = (host_out.nbytes + host_prim.nbytes) / args.steps + 128
+    e2e_ctx.close()
+    # ---- roofline of the dominant pass
+    nky, nkz = info.ky_keep, info.kz_keep
+    pb = pass_bytes(n, info.kx_keep, nky, nkz)
+    launches = args.steps * 3
+    dom = max(range(5), key=lambda i: pass_ms[i])
+    name = PASS_NAMES[dom]
+    avg_ms = pass_ms[dom] / launches
+    achieved = pb[name] / (avg_ms * 1e-3) / 1e9
+    peak, src = peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(name)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32x2 (float-float)" if args.precision == "dd" else "f64",
+        "data": "synthetic (seeded random-phase spectrum, 1<=|k|<=8, rms 0.5, seed 1)",
+        "config": {"workload": WORKLOAD, "grid": n, "variant": "3DC", "precision": args.precision, "hall": 0.05,
+                   "expanding_box": "Ur0/R0=0.01", "dealias": "2/3 sphere", "cfl": 0.4,
+                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (7 GB working set)"},
+        "gpu_launches": args.steps * info.kernels_per_step,
+        "status": status,
+        "graph_ms_per_step": graph_ms,
+        "pass_ms_per_step": {PASS_NAMES[i]: pass_ms[i] / args.steps for i in range(6)},
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": pb[name]},
+        "e2e": {"value": e2e_v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "pinned": pinned},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, cores, sample = cpu_sample(1, 0)
+        line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="dd", choices=["dd", "fp64"])
+    ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
+    ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

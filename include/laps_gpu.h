@@ -140,6 +140,13 @@ int laps_vardt(laps_ctx* ctx, double* dt);
  * values after the last step and *status the OR of the status bits. */
 int laps_step(laps_ctx* ctx, int nsteps, double* time, double* dt, int* status);
 
+/* laps_step without the CUDA graph, with a CUDA event recorded on the context's stream
+ * after every kernel (no host synchronisation inside the region).  pass_ms[0..5] receive the
+ * summed device time of passes A, B, C, D, E (see laps_gb300/csrc/kernels.cuh) and of the
+ * small bookkeeping kernels; *total_ms the event time of the whole region.  For profiling;
+ * it has no counterpart in the reference. */
+int laps_step_profiled(laps_ctx* ctx, int nsteps, double* pass_ms, double* total_ms, int* status);
+
 /* One RK stage irk = 1..3 of evolve with the current dt, for stage-level comparisons
  * (mhd.f90:303-325: calc_flux, transform_flux_real_to_fourier, calc_rhs, rkt, dealias,
  * transform_uu_fourier_to_real, update_uu_prim_from_uu). */

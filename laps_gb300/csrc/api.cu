@@ -110,6 +110,10 @@ int laps_step(laps_ctx* c, int n, double* time, double* dt, int* status) {
   if (n < 0) return fail(c, LAPS_EINVAL, "nsteps < 0");
   return guarded(c, [&] { c->e->step(n, time, dt, status); });
 }
+int laps_step_profiled(laps_ctx* c, int n, double* pass_ms, double* total_ms, int* status) {
+  if (n < 1 || !pass_ms || !total_ms) return fail(c, LAPS_EINVAL, "bad arguments");
+  return guarded(c, [&] { c->e->step_profiled(n, pass_ms, total_ms, status); });
+}
 int laps_rk_stage(laps_ctx* c, int irk) { return guarded(c, [&] { c->e->rk_stage(irk); }); }
 int laps_download_state(laps_ctx* c, double* uu, double* prim) { return guarded(c, [&] { c->e->download(uu, prim); }); }
 int laps_download_spectral(laps_ctx* c, double* uf) {

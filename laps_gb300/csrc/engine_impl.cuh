@@ -58,6 +58,7 @@ class EngineBase {
   virtual void wait(int timeout_ms) = 0;
   virtual void get_time(double* t, double* dt) = 0;
   virtual void info(laps_info* i) = 0;
+  virtual void step_profiled(int n, double* pass_ms, double* total_ms, int* status) = 0;
 };
 
 template <class T> class Engine : public EngineBase {
@@ -233,6 +234,7 @@ template <class T> class Engine : public EngineBase {
   }
 
   ~Engine() override {
+    for (cudaEvent_t ev : ev_pool) cudaEventDestroy(ev);
     if (graph_steady) cudaGraphExecDestroy(graph_steady);
     for (void* a : allocs) cudaFree(a);
     if (h_st) cudaFreeHost(h_st);
@@ -303,20 +305,26 @@ template <class T> class Engine : public EngineBase {
     const Geo& gi = g_in();
     PassArgs ai = args(gi, stage, store_rk, cfl);
     passA(ai);
+    mark(0);
     passB(ai);
+    mark(1);
     // pass C reads the inverse-side ranges and writes the forward-side kx range
     PassArgs ac = ai;
     ac.g.kx_keep = std::max(gi.kx_keep, g_out().kx_keep);
     passC(ac);
+    mark(2);
     if (cfl) {
       k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl);
       LAPS_CK(cudaGetLastError());
+      mark(5);
     }
     PassArgs ao = args(g_out(), stage, store_rk, 0);
     // the first stage after an upload must also clear every mode outside the kept box
     if (!dealiased) ao.g = gfull;
     passD(ao);
+    mark(3);
     passE(ao);
+    mark(4);
     dealiased = true;
   }
   void enqueue_step() {
@@ -326,6 +334,48 @@ template <class T> class Engine : public EngineBase {
     k_advance_time<<<1, 32, 0, stream>>>(st, p.radius0, P.Ur);
     LAPS_CK(cudaGetLastError());
     tables();
+    mark(5);
+  }
+
+  // ---------------------------------------------------------------- profiling marks
+  // When `prof_on`, an event is recorded after every kernel of the step; the time between
+  // consecutive events is attributed to the kernel kind recorded with the later one.
+  bool prof_on = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kind;
+  size_t ev_used = 0;
+  void mark(int kind) {
+    if (!prof_on) return;
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      LAPS_CK(cudaEventCreate(&e));
+      ev_pool.push_back(e);
+      ev_kind.push_back(0);
+    }
+    ev_kind[ev_used] = kind;
+    LAPS_CK(cudaEventRecord(ev_pool[ev_used], stream));
+    ev_used++;
+  }
+  void step_profiled(int n, double* pass_ms, double* total_ms, int* status) override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    LAPS_CK(cudaMemsetAsync(&st->status, 0, sizeof(int), stream));
+    LAPS_CK(cudaMemsetAsync(&st->halt, 0, sizeof(int), stream));
+    prof_on = true;
+    ev_used = 0;
+    mark(-1);
+    for (int i = 0; i < n; i++) enqueue_step();
+    prof_on = false;
+    read_state();
+    for (int k = 0; k < 6; k++) pass_ms[k] = 0.0;
+    for (size_t i = 1; i < ev_used; i++) {
+      float ms = 0.f;
+      LAPS_CK(cudaEventElapsedTime(&ms, ev_pool[i - 1], ev_pool[i]));
+      pass_ms[ev_kind[i]] += ms;
+    }
+    float tot = 0.f;
+    if (ev_used > 1) LAPS_CK(cudaEventElapsedTime(&tot, ev_pool[0], ev_pool[ev_used - 1]));
+    *total_ms = tot;
+    if (status) *status = h_st->status;
   }
 
   void wait(int timeout_ms) override {

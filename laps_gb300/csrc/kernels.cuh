@@ -286,6 +286,7 @@ __global__ void k_tables(const double* __restrict__ wxd, const double* __restric
 // (mhd.f90:418-428, rktmod.f90:15-27).
 static __global__ void k_finalize_dt(StepState* st, double cfl) {
   if (threadIdx.x | blockIdx.x) return;
+  if (st->halt) return;
   double m = __longlong_as_double((long long)st->cfl_bits);
   st->cfl_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
   double dtmin = m * cfl;

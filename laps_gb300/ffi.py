@@ -89,6 +89,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_vardt": (C.c_int, [vp, dp]),
         "laps_step": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
         "laps_rk_stage": (C.c_int, [vp, C.c_int]),
+        "laps_step_profiled": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
         "laps_download_state": (C.c_int, [vp, dp, dp]),
         "laps_download_spectral": (C.c_int, [vp, dp]),
         "laps_upload_spectral": (C.c_int, [vp, dp]),
@@ -177,6 +178,13 @@ class Laps:
         t, d, s = C.c_double(), C.c_double(), C.c_int()
         self._ck(self.lib.laps_step(self.h, int(n), C.byref(t), C.byref(d), C.byref(s)))
         return t.value, d.value, s.value
+
+    def step_profiled(self, n: int):
+        """n steps with per-pass CUDA-event timing: (pass_ms[6], total_ms, status)."""
+        pm = (C.c_double * 6)()
+        tot, s = C.c_double(), C.c_int()
+        self._ck(self.lib.laps_step_profiled(self.h, int(n), pm, C.byref(tot), C.byref(s)))
+        return np.array(pm[:]), tot.value, s.value
 
     def rk_stage(self, irk: int):
         self._ck(self.lib.laps_rk_stage(self.h, int(irk)))

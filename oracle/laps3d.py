@@ -514,3 +514,26 @@ def magnetic_helicity(bf, kx, ky, kz, nx):
     if nx % 2 == 0:
         w[-1] = 1.0
     return float(np.sum(dens * w[None, None, :]))
+
+
+def params_from(n, kw) -> Params3D:
+    """Params3D for an n^3 (or (nx, ny, nz)) grid from C-ABI-style keyword values."""
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    p = Params3D(nx=nx, ny=ny, nz=nz)
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            continue
+        cur = getattr(p, k)
+        setattr(p, k, bool(v) if isinstance(cur, bool) else type(cur)(v))
+    return p
+
+
+def restart(n, kw, prim, t0=0.0) -> Laps3DC:
+    """Start as the reference's restart path does: read primitives, evolve_radius(t0),
+    conserve, forward transform (src_compressible/mhd.f90:101-122)."""
+    o = Laps3DC(params_from(n, kw))
+    o.initial_calc_conserve_variable(prim)
+    o.time = t0
+    o.evolve_radius(t0)
+    o.transform_uu_real_to_fourier()
+    return o

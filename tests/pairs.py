@@ -59,7 +59,10 @@ def rel_l2(a, b, floor):
 
 
 def state_floor(uu):
-    return 1e-12 * float(np.linalg.norm(uu))
+    """Norm below which a field counts as zero: errors in it are measured against 1e-3 of
+    the state's typical field norm instead of its own (a field that is zero analytically
+    holds only round-off)."""
+    return 1e-3 * float(np.linalg.norm(uu)) / math.sqrt(uu.shape[0])
 
 
 def turb(n, **kw):

@@ -148,19 +148,26 @@ def test_diagnostics_match_oracle(prec):
 @pytest.mark.parametrize("prec", PRECS, ids=PREC_ID)
 def test_alfven_wave_known_answer(prec):
     """ipert=1: the circularly polarised Alfven wave travels at v_A = 1 and decays as
-    exp(-eta k^2 t) with eta = nu (mhdinit.f90:328-342)."""
+    exp(-eta k^2 t) with eta = nu (mhdinit.f90:328-342).  The GPU run matches the oracle to
+    round-off, and both match the exact solution within RK3's truncation error (the
+    measured error at this dt is 2.2e-6 of an amplitude 0.1)."""
     n, eta = 16, 1e-2
     kw = dict(if_resis=1, resistivity=eta, if_visc=1, viscosity=eta, dealias_option=1, cfl=0.05)
     prim = alfven(n, db0=0.1)
     o, g = start_pair(n, kw, prim, prec)
     t, dt, st = g.step(40)
+    o.dt = 0.0
+    for _ in range(40):
+        o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    assert abs(t - o.time) <= 1e-13 * t
     uu, _ = g.download_state()
+    assert rel_l2(uu, o.uu, state_floor(o.uu)).max() < 1e-12
     x = np.arange(n) * (2 * math.pi / n)
     dec = math.exp(-eta * t)
     bz = -0.1 * np.sin(x - t) * dec
     by = -0.1 * np.cos(x - t) * dec
-    assert np.abs(uu[6] - bz[None, None, :]).max() < 1e-6
-    assert np.abs(uu[5] - by[None, None, :]).max() < 1e-6
+    assert np.abs(uu[6] - bz[None, None, :]).max() < 1e-5
+    assert np.abs(uu[5] - by[None, None, :]).max() < 1e-5
     assert np.abs(uu[4] - 1.0).max() < 1e-12
 
 
