@@ -1,0 +1,106 @@
+! iso_c_binding interface to liblaps_gpu.so (include/laps_gpu.h) for a Fortran LAPS host.
+! Not compile-checked in this repository (no Fortran compiler is installed here); the types
+! and argument passing follow the C declarations one-for-one.
+module laps_gpu
+    use, intrinsic :: iso_c_binding
+    implicit none
+
+    integer(c_int), parameter :: LAPS_OK = 0
+    integer(c_int), parameter :: LAPS_STATUS_NAN = 1, LAPS_STATUS_DT_FLOOR = 2
+    integer(c_int), parameter :: LAPS_VARIANT_3DC = 0, LAPS_VARIANT_3DI = 1, LAPS_VARIANT_2DC = 2
+    integer(c_int), parameter :: LAPS_PREC_FP64 = 0, LAPS_PREC_DD = 1, LAPS_PREC_FP32 = 2
+    integer(c_int), parameter :: LAPS_LAYOUT_PRIMITIVE = 0, LAPS_LAYOUT_CONSERVED = 1
+
+    type, bind(C) :: laps_params
+        integer(c_int) :: variant, precision
+        integer(c_int) :: nx, ny, nz
+        real(c_double) :: Lx, Ly, Lz
+        real(c_double) :: adiabatic_index
+        integer(c_int) :: if_resis, if_resis_exp
+        real(c_double) :: resistivity
+        integer(c_int) :: if_visc, if_visc_exp
+        real(c_double) :: viscosity
+        integer(c_int) :: if_conserve_background
+        integer(c_int) :: dealias_option
+        real(c_double) :: afx, afy, afz
+        real(c_double) :: cfl
+        integer(c_int) :: if_AEB
+        real(c_double) :: radius0, Ur0
+        integer(c_int) :: if_corotating
+        real(c_double) :: corotating_angle
+        integer(c_int) :: if_Hall
+        real(c_double) :: ion_inertial_length
+        integer(c_int) :: device, timeout_ms
+        integer(c_long_long) :: mem_cap_bytes
+        integer(c_int) :: reserved(8)
+    end type laps_params
+
+    type, bind(C) :: laps_diag
+        real(c_double) :: time, dt, radius
+        real(c_double) :: uu_ave(8), uu_rms(8), rho_u2(3)
+        real(c_double) :: max_divB, e_kin, e_mag, h_cross, h_mag
+    end type laps_diag
+
+    interface
+        integer(c_int) function laps_params_default(p) bind(C, name='laps_params_default')
+            import :: c_int, laps_params
+            type(laps_params), intent(out) :: p
+        end function
+        integer(c_int) function laps_create(p, ctx) bind(C, name='laps_create')
+            import :: c_int, c_ptr, laps_params
+            type(laps_params), intent(in) :: p
+            type(c_ptr), intent(out) :: ctx
+        end function
+        subroutine laps_destroy(ctx) bind(C, name='laps_destroy')
+            import :: c_ptr
+            type(c_ptr), value :: ctx
+        end subroutine
+        integer(c_int) function laps_upload_state(ctx, uu, layout) bind(C, name='laps_upload_state')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(in) :: uu(*)
+            integer(c_int), value :: layout
+        end function
+        integer(c_int) function laps_set_time(ctx, time) bind(C, name='laps_set_time')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), value :: time
+        end function
+        integer(c_int) function laps_vardt(ctx, dt) bind(C, name='laps_vardt')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: dt
+        end function
+        integer(c_int) function laps_step(ctx, nsteps, time, dt, status) bind(C, name='laps_step')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nsteps
+            real(c_double), intent(out) :: time, dt
+            integer(c_int), intent(out) :: status
+        end function
+        integer(c_int) function laps_rk_stage(ctx, irk) bind(C, name='laps_rk_stage')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: irk
+        end function
+        integer(c_int) function laps_download_state(ctx, uu, uu_prim) bind(C, name='laps_download_state')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: uu(*), uu_prim(*)
+        end function
+        integer(c_int) function laps_diagnostics(ctx, d) bind(C, name='laps_diagnostics')
+            import :: c_int, c_ptr, laps_diag
+            type(c_ptr), value :: ctx
+            type(laps_diag), intent(out) :: d
+        end function
+        integer(c_int) function laps_wait(ctx, timeout_ms) bind(C, name='laps_wait')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: timeout_ms
+        end function
+        type(c_ptr) function laps_last_error(ctx) bind(C, name='laps_last_error')
+            import :: c_ptr
+            type(c_ptr), value :: ctx
+        end function
+    end interface
+end module laps_gpu
