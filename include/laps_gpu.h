@@ -166,6 +166,24 @@ int laps_upload_spectral(laps_ctx* ctx, const double* uf);
  * kinetic/magnetic energy, cross- and magnetic helicity of the current state. */
 int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
 
+/* Forward transform of nfields real FP64 fields that allocates no device memory, for hosts
+ * that cannot call cudaMalloc (their device memory comes from their own pool or framework,
+ * or allocation is not allowed after start-up).  No counterpart in the reference: it is the
+ * transform of laps_upload_state (transform_uu_real_to_fourier, fftw.f90:42-71) run on
+ * buffers the caller owns.
+ *   uu: device pointer, uu(nx,ny,nz,nfields) float64;  uf: device pointer,
+ *   uu_fourier(nx/2+1,ny,nz,nfields) interleaved complex float64;  stream: a cudaStream_t
+ *   (NULL: the default stream).  The call is asynchronous on that stream.
+ * The intermediate half spectrum of one field lives in a fixed 32 MiB device array inside
+ * the library, which every GPU that loads the library holds until the process exits; grids
+ * whose padded half spectrum ((nx/2+1 rounded up to 8) * ny * nz) exceeds 2^21 complex
+ * elements - 128^3 fits - are rejected with LAPS_EINVAL.  The first call on a device looks
+ * up the array's address with that device current; make that first call before any stream
+ * capture.  Every call shares the array, so calls that overlap on the GPU (other streams,
+ * other host threads) race.  Errors are reported through laps_last_error(NULL). */
+int laps_transform_uu_real_to_fourier_noalloc(const double* uu, double* uf, int nx, int ny, int nz, int nfields,
+                                              void* stream);
+
 /* Bounded wait for all queued work of the context. */
 int laps_wait(laps_ctx* ctx, int timeout_ms);
 

@@ -19,6 +19,9 @@ struct laps_ctx {
 
 static thread_local std::string g_create_err;
 
+// used by entry points that have no context
+void laps_set_create_error(const std::string& m) { g_create_err = m; }
+
 static int fail(laps_ctx* c, int code, const std::string& m) {
   if (c) c->err = m;
   else g_create_err = m;
