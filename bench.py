@@ -67,9 +67,10 @@ def barrier(ws):
         dist.barrier()
 
 
-def initial_state(n=N_GRID):
+def initial_state(n=None):
     from laps_gb300.ic import turbulence_ic
 
+    n = n or N_GRID
     return turbulence_ic(n, kmin=1, kmax=8, alpha=-1.0, rms_u=0.5, rms_b=0.5, seed=1)
 
 
@@ -145,11 +146,12 @@ def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, elem=16):
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 
-def cpu_sample(steps, warmup, n=N_GRID):
+def cpu_sample(steps, warmup, n=None):
     """The oracle restatement of the reference's step on the host cores: warmup + timed steps
     at the full grid.  Returns (grid-point-steps/s, threads, sample text)."""
     from oracle import laps3d
 
+    n = n or N_GRID
     o = laps3d.restart(n, CFG2, initial_state(n))
     for _ in range(warmup):
         o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
@@ -291,6 +293,7 @@ def run_ours(args):
 
 
 def main():
+    global N_GRID, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -299,7 +302,11 @@ def main():
     ap.add_argument("--precision", default="dd", choices=["dd", "fp64"])
     ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
     ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")
+    ap.add_argument("--grid", type=int, default=256, help="grid size n (n^3); the headline workload is 256")
     args = ap.parse_args()
+    if args.grid != N_GRID:
+        N_GRID = args.grid
+        WORKLOAD = f"3D compressible Hall-MHD + expanding box, {N_GRID}^3 (reduced case)"
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

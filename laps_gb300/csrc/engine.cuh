@@ -3,7 +3,7 @@
 // wave-number tables and the pointwise physics of the 3-D compressible equations.
 #pragma once
 #include "fft.cuh"
-#include "../../include/laps_gpu.h"
+#include "laps_gpu.h"
 
 namespace laps {
 

@@ -130,10 +130,17 @@ __device__ __forceinline__ cx<T> twiddle(const typename Store<T>::C* __restrict_
   return DIR < 0 ? w : conj(w);
 }
 
-// One Stockham stage of radix R after NS points have been combined, for every line of the
-// tile.  Thread t of line l; threads with active == false only join the two barriers.
-template <class T, int N, int DIR, int R, int NS, int JS, int LS>
-__device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t, bool active,
+// Shared-memory position of element j of a line: columns use j*JS; rows (JS == 1) are
+// padded by one element after every 16 so that the radix-16 write pattern (stride 16
+// elements) spreads over all banks.
+template <int JS> __device__ __forceinline__ int sm_idx(int j) { return JS == 1 ? j + (j >> 4) : j * JS; }
+template <int N> struct RowLen { static constexpr int V = N + N / 16; };  // padded length of a row line
+
+// One Stockham stage of radix R after ns points have been combined (ns a power of two, 1
+// for the first stage: no twiddles), for every line of the tile.  Thread t of line l;
+// threads with active == false only join the two barriers.
+template <class T, int N, int DIR, int R, int JS, int LS>
+__device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t, bool active, int ns, int lns,
                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
   using P = Plan<N>;
   constexpr int NB = P::EPT / R;  // butterflies per thread
@@ -144,10 +151,10 @@ __device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t,
     for (int q = 0; q < NB; q++) {
       int b = t + q * P::TPL;
 #pragma unroll
-      for (int i = 0; i < R; i++) v[q][i] = Store<T>::ldc(line + (b + i * (N / R)) * JS);
-      if (NS > 1) {
-        int k = b % NS;
-        int step = k * (N / (NS * R)) * twstep;
+      for (int i = 0; i < R; i++) v[q][i] = Store<T>::ldc(line + sm_idx<JS>(b + i * (N / R)));
+      if (ns > 1) {
+        int k = b & (ns - 1);
+        int step = (k * (N / R) >> lns) * twstep;  // k * N / (ns R)
 #pragma unroll
         for (int i = 1; i < R; i++) v[q][i] = v[q][i] * twiddle<T, DIR>(tw, i * step);
       }
@@ -158,30 +165,34 @@ __device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t,
 #pragma unroll
     for (int q = 0; q < NB; q++) {
       int b = t + q * P::TPL;
-      int k = b % NS;
+      int k = b & (ns - 1);
       dft_r<T, DIR, R>(v[q]);
-      int base = (b / NS) * NS * R + k;
+      int base = ((b >> lns) << lns) * R + k;
 #pragma unroll
-      for (int i = 0; i < R; i++) Store<T>::stc(line + (base + i * NS) * JS, v[q][i]);
+      for (int i = 0; i < R; i++) Store<T>::stc(line + sm_idx<JS>(base + i * ns), v[q][i]);
     }
   }
   __syncthreads();
 }
 
 // Full FFT of every line of the tile (unnormalised).  Every thread of the block calls it.
-// tw: table of exp(-2 pi i j / (N*twstep)), j = 0..N*twstep-1.
+// The radix-16 stages run in a rolled loop (one copy of their code); the last radix-2/4/8
+// stage follows.  tw: table of exp(-2 pi i j / (N*twstep)), j = 0..N*twstep-1.
 template <class T, int N, int DIR, int JS, int LS>
 __device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t, bool active,
                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
   using P = Plan<N>;
   if constexpr (N < 16) {
-    fft_stage<T, N, DIR, N, 1, JS, LS>(s, l, t, active, tw, twstep);
+    fft_stage<T, N, DIR, N, JS, LS>(s, l, t, active, 1, 0, tw, twstep);
   } else {
-    fft_stage<T, N, DIR, 16, 1, JS, LS>(s, l, t, active, tw, twstep);
-    if constexpr (P::NS16 >= 2) fft_stage<T, N, DIR, 16, 16, JS, LS>(s, l, t, active, tw, twstep);
-    if constexpr (P::NS16 >= 3) fft_stage<T, N, DIR, 16, 256, JS, LS>(s, l, t, active, tw, twstep);
-    constexpr int NSR = P::NS16 == 1 ? 16 : P::NS16 == 2 ? 256 : 4096;
-    if constexpr (P::REST > 1) fft_stage<T, N, DIR, P::REST, NSR, JS, LS>(s, l, t, active, tw, twstep);
+    int ns = 1, lns = 0;
+#pragma unroll 1
+    for (int st = 0; st < P::NS16; st++) {
+      fft_stage<T, N, DIR, 16, JS, LS>(s, l, t, active, ns, lns, tw, twstep);
+      ns <<= 4;
+      lns += 4;
+    }
+    if constexpr (P::REST > 1) fft_stage<T, N, DIR, P::REST, JS, LS>(s, l, t, active, ns, lns, tw, twstep);
   }
 }
 

@@ -27,7 +27,7 @@ template <class T, int N> struct Col {
   static constexpr int NTILE = NT >= 128 ? 1 : 128 / NT;
   static constexpr int THREADS = NT * NTILE;
   static constexpr int EPT = N / TPL;  // elements per thread
-  static constexpr int SMEM = NTILE * N * TX * (int)sizeof(C);
+  static constexpr int SMEM = NTILE * N * TX * (int)sizeof(C);  // one buffer per tile
 };
 
 template <class T> struct Bufs {
@@ -74,12 +74,16 @@ __global__ void __launch_bounds__(Col<T, N>::THREADS)
   }
 }
 
-// Row helpers: a real row of NX values viewed as NX/2 complex (x[2m] + i x[2m+1]).
+// Row helpers: a real row of NX values viewed as NX/2 complex (x[2m] + i x[2m+1]), stored
+// in shared memory with one padding element after every 16 complex (sm_idx<1>).
 template <int NX> struct RowP {
   static constexpr int H = NX / 2;
   static constexpr int TPL = Plan<H>::TPL;
   static constexpr int LB = 128 / TPL >= 1 ? 128 / TPL : 1;  // lines per batch of 128 threads
+  static constexpr int LC = RowLen<H>::V;                    // padded line length (complex)
 };
+// real x of a padded row line, in Store<T>::R units
+__device__ __forceinline__ int row_real_idx(int x) { return 2 * sm_idx<1>(x >> 1) + (x & 1); }
 
 // c2r pre-processing of one line: Z[k] = (X[k] + conj X[h-k]) + i conj(W^k) (X[k] - conj X[h-k])
 // for the pair (k, h-k); X read from global through `ldx`, imaginary parts of X[0], X[h] ignored.
@@ -97,8 +101,8 @@ __device__ __forceinline__ void c2r_pre(typename Store<T>::C* z, int t, LDX ldx,
     } else {
       cx<T> wb = conj(Store<T>::ldg(twx + k2));
       cx<T> zb = (b + conj(a)) + times_i(wb * (b - conj(a)));
-      Store<T>::stc(z + k, za);
-      if (k2 != k) Store<T>::stc(z + k2, zb);
+      Store<T>::stc(z + sm_idx<1>(k), za);
+      if (k2 != k) Store<T>::stc(z + sm_idx<1>(k2), zb);
     }
   }
 }
@@ -119,7 +123,7 @@ __device__ __forceinline__ void r2c_post(const typename Store<T>::C* z, int t, S
       continue;
     }
     int k2 = H - k;
-    cx<T> a = Store<T>::ldc(z + k), b = Store<T>::ldc(z + k2);
+    cx<T> a = Store<T>::ldc(z + sm_idx<1>(k)), b = Store<T>::ldc(z + sm_idx<1>(k2));
     cx<T> wa = Store<T>::ldg(twx + k);
     cx<T> xa = (a + conj(b)) - times_i(wa * (a - conj(b)));
     xa = {Real<T>::mul_pow2(xa.re, scale_exp - 1), Real<T>::mul_pow2(xa.im, scale_exp - 1)};
@@ -141,16 +145,18 @@ __global__ void __launch_bounds__(128) k_row_r2c(const typename Store<T>::R* __r
   using C = typename Store<T>::C;
   using SR = typename Store<T>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sc = reinterpret_cast<C*>(smem_raw);
   SR* sr = reinterpret_cast<SR*>(smem_raw);
   long long row0 = (long long)blockIdx.x * RP::LB;
   for (int i = threadIdx.x; i < RP::LB * NX; i += blockDim.x) {
-    long long r = row0 + i / NX;
-    sr[i] = r < nrows ? in[r * NX + i % NX] : SR{};
+    int l = i / NX, x = i % NX;
+    long long r = row0 + l;
+    sr[2 * l * RP::LC + row_real_idx(x)] = r < nrows ? in[r * NX + x] : SR{};
   }
   __syncthreads();
   int l = threadIdx.x / RP::TPL, t = threadIdx.x % RP::TPL;
   bool act = l < RP::LB;
-  C* z = reinterpret_cast<C*>(sr + (act ? l : 0) * NX);
+  C* z = sc + (act ? l : 0) * RP::LC;
   fft_lines<T, RP::H, -1, 1, 0>(z, 0, t, act, twx, 2);
   long long r = row0 + l;
   if (!act || r >= nrows) return;
@@ -166,11 +172,12 @@ __global__ void __launch_bounds__(128) k_row_c2r(const typename Store<T>::C* __r
   using C = typename Store<T>::C;
   using SR = typename Store<T>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sc = reinterpret_cast<C*>(smem_raw);
   SR* sr = reinterpret_cast<SR*>(smem_raw);
   long long row0 = (long long)blockIdx.x * RP::LB;
   int l = threadIdx.x / RP::TPL, t = threadIdx.x % RP::TPL;
   bool act = l < RP::LB && row0 + l < nrows;
-  C* z = reinterpret_cast<C*>(sr + (l < RP::LB ? l : 0) * NX);
+  C* z = sc + (l < RP::LB ? l : 0) * RP::LC;
   if (act) {
     const C* x = in + (row0 + l) * kxp;
     c2r_pre<T, RP::H>(z, t, [&](int k) { return Store<T>::ldg(x + k); }, twx);
@@ -178,8 +185,9 @@ __global__ void __launch_bounds__(128) k_row_c2r(const typename Store<T>::C* __r
   __syncthreads();
   fft_lines<T, RP::H, +1, 1, 0>(z, 0, t, l < RP::LB, twx, 2);
   for (int i = threadIdx.x; i < RP::LB * NX; i += blockDim.x) {
-    long long r = row0 + i / NX;
-    if (r < nrows) out[r * NX + i % NX] = sr[i];
+    int ll = i / NX, x = i % NX;
+    long long r = row0 + ll;
+    if (r < nrows) out[r * NX + x] = sr[2 * ll * RP::LC + row_real_idx(x)];
   }
 }
 

@@ -30,7 +30,7 @@ void launch_rows_r2c(cudaStream_t stream, int nx, const typename Store<T>::R* in
                      const typename Store<T>::C* twx) {
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
-    int sm = RowP<NN>::LB * NN * (int)sizeof(typename Store<T>::R);                                                     \
+    int sm = RowP<NN>::LB * RowP<NN>::LC * (int)sizeof(typename Store<T>::C);                                                   \
     set_smem(k_row_r2c<T, NN>, sm);                                                                                     \
     k_row_r2c<T, NN><<<(unsigned)((nrows + RowP<NN>::LB - 1) / RowP<NN>::LB), 128, sm, stream>>>(in, out, nrows, kxp, -ilog2(NN), twx); \
     break;                                                                                                              \
@@ -45,7 +45,7 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
                      const typename Store<T>::C* twx) {
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
-    int sm = RowP<NN>::LB * NN * (int)sizeof(typename Store<T>::R);                                                     \
+    int sm = RowP<NN>::LB * RowP<NN>::LC * (int)sizeof(typename Store<T>::C);                                                   \
     set_smem(k_row_c2r<T, NN>, sm);                                                                                     \
     k_row_c2r<T, NN><<<(unsigned)((nrows + RowP<NN>::LB - 1) / RowP<NN>::LB), 128, sm, stream>>>(in, out, nrows, kxp, twx); \
     break;                                                                                                              \
@@ -65,7 +65,7 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passA<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE);                                    \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, a.hall ? 10 : 8);                    \
     k_passA<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
     break;                                                                                                              \
   }
@@ -75,7 +75,7 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passB<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE);                                       \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.hall ? 11 : 8);                       \
     k_passB<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
     break;                                                                                                              \
   }
@@ -84,9 +84,9 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passD<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE);                                       \
-    k_passD<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    set_smem(k_passD<T, NN>, 2 * CL::SMEM);                                                                             \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, 12);                                    \
+    k_passD<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passD, k_passD, nz)
@@ -94,9 +94,9 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passE<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE);                                    \
-    k_passE<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    set_smem(k_passE<T, NN>, 2 * CL::SMEM);                                                                             \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, 8);                                  \
+    k_passE<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passE, k_passE, nky)
@@ -108,10 +108,14 @@ void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, c
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CF = PassCCfg<NN>;                                                                                            \
-    int sm = CF::ROWS * CF::NF * NN * (int)sizeof(typename Store<T>::R);                                                \
-    set_smem(k_passC<T, NN>, sm);                                                                                       \
-    long long rows = (long long)a.g.ny * a.g.nz;                                                                        \
-    k_passC<T, NN><<<(unsigned)(rows / CF::ROWS), 128, sm, stream>>>(B, a, pc, tw);                                     \
+    unsigned nb = (unsigned)((long long)a.g.ny * a.g.nz / CF::ROWS);                                                    \
+    if (a.cfl) {                                                                                                        \
+      set_smem(k_passC<T, NN, 1>, CF::SMEM);                                                                            \
+      k_passC<T, NN, 1><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                           \
+    } else {                                                                                                            \
+      set_smem(k_passC<T, NN, 0>, CF::SMEM);                                                                            \
+      k_passC<T, NN, 0><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                           \
+    }                                                                                                                   \
     break;                                                                                                              \
   }
   switch (N) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }
