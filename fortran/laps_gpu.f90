@@ -30,6 +30,8 @@ module laps_gpu
         real(c_double) :: corotating_angle
         integer(c_int) :: if_Hall
         real(c_double) :: ion_inertial_length
+        real(c_double) :: rho0
+        integer(c_int) :: if_z_radial, if_limit_dt_increase, dstep_calcdt
         integer(c_int) :: device, timeout_ms
         integer(c_long_long) :: mem_cap_bytes
         integer(c_int) :: reserved(8)
@@ -38,7 +40,7 @@ module laps_gpu
     type, bind(C) :: laps_diag
         real(c_double) :: time, dt, radius
         real(c_double) :: uu_ave(8), uu_rms(8), rho_u2(3)
-        real(c_double) :: max_divB, e_kin, e_mag, h_cross, h_mag
+        real(c_double) :: max_divB, max_divB_real, max_divV_real, e_kin, e_mag, h_cross, h_mag
     end type laps_diag
 
     interface

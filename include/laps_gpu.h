@@ -48,7 +48,7 @@ extern "C" {
 /* arithmetic of the transforms and the right-hand side */
 #define LAPS_PREC_FP64 0 /* native IEEE binary64 everywhere */
 #define LAPS_PREC_DD 1   /* float-float (two FP32, ~48-bit significand) on the FP32 pipes */
-#define LAPS_PREC_FP32 2 /* FP32 transforms and products, float-float RK accumulation */
+#define LAPS_PREC_FP32 2 /* reserved: FP32 transforms and products */
 
 /* state layouts for laps_upload_state */
 #define LAPS_LAYOUT_PRIMITIVE 0 /* rho, ux, uy, uz, Bx, By, Bz, p (what outNNN.dat holds) */
@@ -79,6 +79,13 @@ typedef struct laps_params {
   double corotating_angle;
   int if_Hall;
   double ion_inertial_length;
+  double rho0;            /* 3-D incompressible: background density dividing grad(rho u)
+                             (src_incompressible/mhdinit.f90:15, default 1) */
+  int if_z_radial;        /* 2-D: z is the radial direction of the expanding box
+                             (src_compressible/2D/mhd.f90:42) */
+  int if_limit_dt_increase; /* 2-D: dt may only decrease (src_compressible/2D/mhd.f90:23) */
+  int dstep_calcdt;       /* 2-D: vardt every dstep_calcdt steps (default 20,
+                             src_compressible/2D/mhd.f90:20); 3-D variants use 1 */
   int device;             /* CUDA device ordinal */
   int timeout_ms;         /* bound on every device wait (default 600000) */
   long long mem_cap_bytes;/* refuse to allocate more than this (0: no cap) */
@@ -95,6 +102,8 @@ typedef struct laps_diag {
   double uu_rms[8];  /* <f^2> - <f>^2 for the same eight                         */
   double rho_u2[3];  /* <rho (u_i - <u_i>)^2>                                    */
   double max_divB;   /* max |i k . B_hat| over the spectral grid                 */
+  double max_divB_real; /* max |div B| on the grid (src_incompressible/mhd.f90:672-700) */
+  double max_divV_real; /* max |div(rho u)| / rho0 on the grid (:701-732)      */
   double e_kin;      /* <rho u^2>/2 */
   double e_mag;      /* <B^2>/2     */
   double h_cross;    /* <u . B>     */

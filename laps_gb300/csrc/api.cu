@@ -57,20 +57,31 @@ int laps_params_default(laps_params* p) {
   p->afx = p->afy = p->afz = 0.495;    // dealiasing.f90:12
   p->cfl = 0.5;                        // mhd.f90:21
   p->radius0 = 30.0;                   // AEBmod.f90:12
+  p->rho0 = 1.0;                       // src_incompressible/mhdinit.f90:15
+  p->dstep_calcdt = 20;                // src_compressible/2D/mhd.f90:20 (2-D only)
   p->timeout_ms = 600000;
   return LAPS_OK;
 }
 
-static bool size_ok(int n, int lo) { return n >= lo && n <= 512 && (n & (n - 1)) == 0; }
+static bool size_ok(int n, int lo) { return n >= lo && n <= 1024 && (n & (n - 1)) == 0; }
 
 int laps_create(const laps_params* p, laps_ctx** out) {
   if (!p || !out) return fail(nullptr, LAPS_EINVAL, "null argument");
   *out = nullptr;
-  if (p->variant != LAPS_VARIANT_3DC) return fail(nullptr, LAPS_EINVAL, "only the 3-D compressible variant is built in this library");
+  if (p->variant != LAPS_VARIANT_3DC && p->variant != LAPS_VARIANT_3DI && p->variant != LAPS_VARIANT_2DC)
+    return fail(nullptr, LAPS_EINVAL, "variant must be LAPS_VARIANT_3DC, LAPS_VARIANT_3DI or LAPS_VARIANT_2DC");
   if (p->precision != LAPS_PREC_FP64 && p->precision != LAPS_PREC_DD)
     return fail(nullptr, LAPS_EINVAL, "precision must be LAPS_PREC_FP64 or LAPS_PREC_DD");
-  if (!size_ok(p->nx, 16) || !size_ok(p->ny, 8) || !size_ok(p->nz, 8))
-    return fail(nullptr, LAPS_EINVAL, "nx must be a power of two in [16,512], ny and nz in [8,512]");
+  if (p->variant == LAPS_VARIANT_2DC) {
+    if (!size_ok(p->nx, 16) || !size_ok(p->ny, 8) || p->nz != 1)
+      return fail(nullptr, LAPS_EINVAL, "2-D: nx a power of two in [16,1024], ny in [8,1024], nz = 1");
+    if (p->dstep_calcdt < 1) return fail(nullptr, LAPS_EINVAL, "dstep_calcdt must be >= 1");
+    if (p->if_AEB && p->if_z_radial && p->if_corotating)
+      return fail(nullptr, LAPS_EINVAL, "if_z_radial and if_corotating cannot both be set (src_compressible/2D/mhd.f90:59-68)");
+  } else if (!size_ok(p->nx, 16) || !size_ok(p->ny, 8) || !size_ok(p->nz, 8) || p->nx > 512 || p->ny > 512 || p->nz > 512) {
+    return fail(nullptr, LAPS_EINVAL, "3-D: nx a power of two in [16,512], ny and nz in [8,512]");
+  }
+  if (p->variant == LAPS_VARIANT_3DI && !(p->rho0 > 0)) return fail(nullptr, LAPS_EINVAL, "rho0 must be positive");
   if (!(p->Lx > 0 && p->Ly > 0 && p->Lz > 0)) return fail(nullptr, LAPS_EINVAL, "box lengths must be positive");
   if (!(p->adiabatic_index != 1.0) || !(p->cfl > 0)) return fail(nullptr, LAPS_EINVAL, "adiabatic_index must differ from 1 and cfl be positive");
   if (p->if_AEB && !(p->radius0 > 0)) return fail(nullptr, LAPS_EINVAL, "radius0 must be positive");

@@ -27,7 +27,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* out) {
 // sums of rho, ux, uy, uz, Bx, By, Bz, p, their squares, rho u^2, B^2 and u.B
 template <class T>
 __global__ void __launch_bounds__(256) k_diag_sums(const typename Store<T>::R* __restrict__ u, long long n, double gamma,
-                                                   double* part) {
+                                                   int incomp, double* part) {
   double v[19];
 #pragma unroll
   for (int k = 0; k < 19; k++) v[k] = 0.0;
@@ -36,7 +36,9 @@ __global__ void __launch_bounds__(256) k_diag_sums(const typename Store<T>::R* _
 #pragma unroll
     for (int f = 0; f < 8; f++) q[f] = Real<T>::to_d(Store<T>::ld(u + f * n + i));
     double ux = q[1] / q[0], uy = q[2] / q[0], uz = q[3] / q[0];
-    double p = (q[7] - 0.5 * (q[1] * ux + q[2] * uy + q[3] * uz + q[4] * q[4] + q[5] * q[5] + q[6] * q[6])) * (gamma - 1);
+    // the incompressible state holds p itself in slot 8; the reference's rms there reads
+    // uu_prim(:,:,:,4) beyond its 3 components (src_incompressible/mhdrms.f90:73,83)
+    double p = incomp ? q[7] : (q[7] - 0.5 * (q[1] * ux + q[2] * uy + q[3] * uz + q[4] * q[4] + q[5] * q[5] + q[6] * q[6])) * (gamma - 1);
     double f8[8] = {q[0], ux, uy, uz, q[4], q[5], q[6], p};
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -110,6 +112,47 @@ __global__ void __launch_bounds__(256) k_diag_spec(const typename Store<T>::C* _
     double m = 0;
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = fmax(m, rm[i]);
     part[(size_t)blockIdx.x * 2] = m;
+  }
+}
+
+// i (ax X + ay Y + az Z) * scale of three state slots, written with the spectral pitch:
+// div B (slots 4..6) or div(rho u) / rho0 (slots 1..3) before the inverse transform of
+// calc_divB_real / calc_divV_real (src_incompressible/mhdrhs.f90:532-648)
+template <class T>
+__global__ void k_spec_div(const typename Store<T>::C* __restrict__ U, typename Store<T>::C* __restrict__ out, Geo g, KTab<T> K,
+                           Phys P, PT<T> pc, const StepState* st, int first, int scale_by_rho0) {
+  long long tot = (long long)g.nz * g.ny * g.kxp;
+  T rr = Real<T>::from_d(st->r_ratio);
+  T sc = Real<T>::from_d(scale_by_rho0 ? 1.0 / st->rho0 : 1.0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    int kx = i % g.kxp;
+    long long r = i / g.kxp;
+    int ky = r % g.ny, kz = r / g.ny;
+    cx<T> v = cx_zero<T>();
+    if (kx < g.nh) {
+      T ax, ay, az;
+      kfac(K, P, pc, rr, kx, ky, kz, ax, ay, az);
+      v = (mul_i(Store<T>::ldc(U + first * g.fsc + i), ax) + mul_i(Store<T>::ldc(U + (first + 1) * g.fsc + i), ay)) +
+          mul_i(Store<T>::ldc(U + (first + 2) * g.fsc + i), az);
+      if (scale_by_rho0) v = v * sc;
+    }
+    Store<T>::stc(out + i, v);
+  }
+}
+
+// per-block max |x| of one real field
+template <class T>
+__global__ void __launch_bounds__(256) k_max_abs(const typename Store<T>::R* __restrict__ u, long long n, double* part) {
+  double m = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    m = fmax(m, fabs(Real<T>::to_d(Store<T>::ld(u + i))));
+  __shared__ double rm[8];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) rm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmax(m, rm[i]);
+    part[blockIdx.x] = fmax(rm[0], m);
   }
 }
 

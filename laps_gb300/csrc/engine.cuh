@@ -37,6 +37,8 @@ struct StepState {
   double inv_tau;                  // 1 / tau_exp (0 when the expanding box is off)
   double r_ratio;                  // radius0 / radius
   unsigned long long cfl_bits;     // running min of the CFL time step (bits of a double)
+  double rho0;                     // 3-D incompressible background density (update_rho_p)
+  long long istep;                 // steps taken (2-D vardt cadence)
   int status;                      // LAPS_STATUS_* bits
   int halt;                        // skip the rest of the step (dt floor)
   int ksq_plain;                   // k^2 still the grid_initialize sum (no R factor)
@@ -46,6 +48,7 @@ struct StepState {
 // wave-number tables (element type T), rebuilt by a small kernel whenever R changes
 template <class T> struct KTab {
   const T* wx;   // kx (nh)
+  const T* kxd;  // kx derivative factor: kx, or kx * R0 / R when z is radial (2-D)
   const T* wy;   // ky (ny) unscaled
   const T* kyd;  // ky * R0 / R   (derivative factor)
   const T* kzd;  // kz * R0 / R
@@ -62,15 +65,21 @@ template <class T> struct KTab {
 struct Phys {
   double gamma, nu, eta, di, cfl, dx, dy, dz, mindx, R0, Ur;
   double cos_cor, sin_cor;
-  // corotating k^2 coefficients (set per step from R0/R)
   int visc, visc_exp, resis, resis_exp, cons_bg, aeb, corot, hall, dealias;
+  int variant;   // LAPS_VARIANT_*
+  int two_d;     // nz == 1: kz = 0, no z term in the CFL
+  int zrad;      // 2-D expanding box with z radial
+  int limit_dt;  // 2-D if_limit_dt_increase
+  int dstep;     // vardt cadence (steps)
+  int ebm_mask;  // variables damped by the expansion (bit v)
 };
 
 // the same constants pre-converted to T on the host (a double -> float-float split per
 // element would run on the FP64 pipe)
 template <class T> struct PT {
   T gamma, gm1, cg, di, nu, eta, cosc, sinc, inv_mindx, half, two, one, zero, four, is2, dx, dy, dz;
-  T ebm[8];
+  T eta_dx, eta_dy;  // explicit-resistivity CFL speeds (2-D)
+  T ebm[8];          // expansion damping factor of each variable
 };
 
 // effective derivative factors (i*ax, i*ay, i*az) at spectral index (ix, iy, iz):
@@ -82,7 +91,7 @@ __device__ __forceinline__ void kfac(const KTab<T>& K, const Phys& P, const PT<T
     ax = K.wx[ix] * c.cosc + K.wy[iy] * c.sinc;
     ay = (K.wy[iy] * c.cosc - K.wx[ix] * c.sinc) * rr;
   } else {
-    ax = K.wx[ix];
+    ax = K.kxd[ix];
     ay = K.kyd[iy];
   }
 }

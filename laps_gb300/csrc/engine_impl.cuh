@@ -80,7 +80,7 @@ template <class T> class Engine : public EngineBase {
   std::vector<void*> allocs;
   Bufs<T> B{};
   C *twx = nullptr, *twy = nullptr, *twz = nullptr;
-  SR *t_wx, *t_wy, *t_kyd, *t_kzd, *t_kx2, *t_ky2, *t_kz2, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr;
+  SR *t_wx, *t_kxd, *t_wy, *t_kyd, *t_kzd, *t_kx2, *t_ky2, *t_kz2, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr;
   double *d_wx, *d_wy, *d_wz;
   short* kxlim = nullptr;
   StepState* st = nullptr;
@@ -95,10 +95,11 @@ template <class T> class Engine : public EngineBase {
     return (X*)ptr;
   }
 
+  static int w2_fields(const laps_params& q) { return q.variant == LAPS_VARIANT_3DI ? 19 : 15; }
   static long long plan_bytes(const laps_params& q) {
     long long kxp = ((q.nx / 2 + 1) + 7) / 8 * 8;
     long long fsc = kxp * q.ny * q.nz;
-    return (8 + 8 + 19 + 15) * fsc * (long long)sizeof(C) + (1 << 20);
+    return (8 + 8 + 19 + w2_fields(q)) * fsc * (long long)sizeof(C) + (1 << 20);
   }
 
   explicit Engine(const laps_params& q) : p(q) {
@@ -117,14 +118,18 @@ template <class T> class Engine : public EngineBase {
     P.gamma = q.adiabatic_index;
     P.nu = q.viscosity; P.eta = q.resistivity; P.di = q.ion_inertial_length; P.cfl = q.cfl;
     P.dx = q.Lx / q.nx; P.dy = q.Ly / q.ny; P.dz = q.Lz / q.nz;
-    P.mindx = std::fmin(std::fmin(P.dx, P.dy), P.dz);
+    const bool two_d = q.variant == LAPS_VARIANT_2DC, incomp = q.variant == LAPS_VARIANT_3DI;
+    P.mindx = two_d ? std::fmin(P.dx, P.dy) : std::fmin(std::fmin(P.dx, P.dy), P.dz);
     P.R0 = q.radius0;
     P.Ur = q.if_AEB ? q.Ur0 : 0.0;  // mhd.f90:88-90
     double ang = q.if_corotating ? q.corotating_angle : 0.0;  // AEBmod.f90:28-30
     P.cos_cor = std::cos(ang); P.sin_cor = std::sin(ang);
     P.visc = q.if_visc; P.visc_exp = q.if_visc_exp; P.resis = q.if_resis; P.resis_exp = q.if_resis_exp;
     P.cons_bg = q.if_conserve_background; P.aeb = q.if_AEB; P.corot = q.if_AEB && q.if_corotating;
-    P.hall = q.if_Hall; P.dealias = (q.dealias_option == 1 || q.dealias_option == 2) ? q.dealias_option : 0;
+    P.hall = q.if_Hall;
+    P.dealias = (q.dealias_option == 1 || q.dealias_option == 2 || (two_d && q.dealias_option == 3)) ? q.dealias_option : 0;
+    P.variant = q.variant; P.two_d = two_d; P.zrad = two_d && q.if_AEB && q.if_z_radial;
+    P.limit_dt = two_d && q.if_limit_dt_increase; P.dstep = two_d ? q.dstep_calcdt : 1;
     pc.gamma = host_cvt<T>(P.gamma); pc.gm1 = host_cvt<T>(P.gamma - 1.0);
     pc.cg = host_cvt<T>(-2.0 * P.gamma / (P.gamma - 1.0));
     pc.di = host_cvt<T>(P.di); pc.nu = host_cvt<T>(P.nu); pc.eta = host_cvt<T>(P.eta);
@@ -134,7 +139,13 @@ template <class T> class Engine : public EngineBase {
     pc.zero = host_cvt<T>(0.0); pc.four = host_cvt<T>(4.0);
     pc.is2 = host_cvt<T>(0.70710678118654752440L);
     pc.dx = host_cvt<T>(P.dx); pc.dy = host_cvt<T>(P.dy); pc.dz = host_cvt<T>(P.dz);
-    const double ebm[8] = {2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 0.0};  // mhdrhs.f90:237-247
+    pc.eta_dx = host_cvt<T>(P.eta / P.dx); pc.eta_dy = host_cvt<T>(P.eta / P.dy);
+    // expansion damping of each variable: mhdrhs.f90:237-247; 2D/mhdrhs.f90:319-343 (radial z);
+    // src_incompressible/mhdrhs.f90:187-204 (p decays with 2 gamma)
+    double ebm[8] = {2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 0.0};
+    if (P.zrad) { double zr[8] = {2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 2.0, 0.0}; std::memcpy(ebm, zr, sizeof ebm); }
+    if (incomp) ebm[7] = 2.0 * P.gamma;
+    P.ebm_mask = incomp ? 0xFF : 0x7F;
     for (int v = 0; v < 8; v++) pc.ebm[v] = host_cvt<T>(ebm[v]);
 
     // wave numbers, mhdinit.f90:88-115 (the Nyquist index takes +k)
@@ -149,16 +160,22 @@ template <class T> class Engine : public EngineBase {
     // dealias option 1: kept kx count per (kz, ky) row with the reference's own formula
     // (dealiasing.f90:87-99), and the box that holds every kept mode
     std::vector<short> lim;
-    if (P.dealias == 1) {
+    if (P.dealias == 1 || P.dealias == 3) {
       lim.assign((size_t)q.nz * q.ny, 0);
       int kxk = 0, kyk = 0, kzk = 0;
       for (int iz = 0; iz < q.nz; iz++)
         for (int iy = 0; iy < q.ny; iy++) {
           int cnt = 0;
           for (int ix = 0; ix < g.nh; ix++) {
-            double r = std::sqrt(std::pow(wx[ix] * q.Lx / (2 * pi * q.nx), 2) + std::pow(wy[iy] * q.Ly / (2 * pi * q.ny), 2) +
-                                 std::pow(wz[iz] * q.Lz / (2 * pi * q.nz), 2));
-            if (!(r > 1.0 / 3.0)) {
+            double rx = wx[ix] * q.Lx / (2 * pi * q.nx), ry = wy[iy] * q.Ly / (2 * pi * q.ny);
+            bool drop;
+            if (two_d && P.dealias == 3)  // square truncation, 2D/dealiasing.f90:102-117
+              drop = std::fabs(rx) > 1.0 / 3.0 || std::fabs(ry) > 1.0 / 3.0;
+            else if (two_d)  // circle, 2D/dealiasing.f90:87-99
+              drop = std::sqrt(std::pow(rx, 2) + std::pow(ry, 2)) > 1.0 / 3.0;
+            else  // sphere, dealiasing.f90:87-99
+              drop = std::sqrt(std::pow(rx, 2) + std::pow(ry, 2) + std::pow(wz[iz] * q.Lz / (2 * pi * q.nz), 2)) > 1.0 / 3.0;
+            if (!drop) {
               if (cnt != ix) throw Error{LAPS_EINVAL, "dealias mask is not monotone in kx"};
               cnt = ix + 1;
               int my = iy <= q.ny / 2 ? iy : q.ny - iy, mz = iz <= q.nz / 2 ? iz : q.nz - iz;
@@ -183,8 +200,8 @@ template <class T> class Engine : public EngineBase {
     B.U = dalloc<C>(8 * g.fsc);
     B.R = dalloc<C>(8 * g.fsc);
     B.W1 = dalloc<C>(19 * g.fsc);
-    B.W2 = dalloc<C>(15 * g.fsc);
-    bytes = (8 + 8 + 19 + 15) * g.fsc * (long long)sizeof(C);
+    B.W2 = dalloc<C>(w2_fields(q) * g.fsc);
+    bytes = (8 + 8 + 19 + w2_fields(q)) * g.fsc * (long long)sizeof(C);
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(C), stream));
     LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
     auto up = [&](auto* dst, const auto& src) {
@@ -197,10 +214,10 @@ template <class T> class Engine : public EngineBase {
     d_wx = dalloc<double>(g.nh); up(d_wx, wx);
     d_wy = dalloc<double>(q.ny); up(d_wy, wy);
     d_wz = dalloc<double>(q.nz); up(d_wz, wz);
-    t_wx = dalloc<SR>(g.nh); t_kx2 = dalloc<SR>(g.nh);
+    t_wx = dalloc<SR>(g.nh); t_kxd = dalloc<SR>(g.nh); t_kx2 = dalloc<SR>(g.nh);
     t_wy = dalloc<SR>(q.ny); t_kyd = dalloc<SR>(q.ny); t_ky2 = dalloc<SR>(q.ny);
     t_kzd = dalloc<SR>(q.nz); t_kz2 = dalloc<SR>(q.nz);
-    if (P.dealias == 1) { kxlim = dalloc<short>(lim.size()); up(kxlim, lim); }
+    if (P.dealias == 1 || P.dealias == 3) { kxlim = dalloc<short>(lim.size()); up(kxlim, lim); }
     if (P.dealias == 2) {  // dealiasing.f90:31-65
       auto filt = [&](const std::vector<double>& w, double L, int n, double af) {
         double aj = (5.0 + 6.0 * af) / 8.0, bj = (1.0 + 2.0 * af) / 2.0, cj = -(1.0 - 2 * af) / 8.0;
@@ -218,6 +235,8 @@ template <class T> class Engine : public EngineBase {
       t_fy = dalloc<SR>(fy.size()); up(t_fy, fy);
       t_fz = dalloc<SR>(fz.size()); up(t_fz, fz);
     }
+    if ((P.dealias == 1 || P.dealias == 3) && !kxlim) throw Error{LAPS_EINVAL, "dealias table missing"};
+    if (P.dealias == 2 && !(t_fx && t_fy && t_fz)) throw Error{LAPS_EINVAL, "dealias filters missing"};
     st = dalloc<StepState>(1);
     LAPS_CK(cudaMallocHost(&h_st, sizeof(StepState)));
     StepState s0{};
@@ -226,6 +245,8 @@ template <class T> class Engine : public EngineBase {
     s0.r_ratio = 1.0;  // radius0 / radius at start; the factor itself is (k R0)/R below
     s0.cfl_bits = 0x7FF0000000000000ull;
     s0.ksq_plain = 1;  // grid_initialize's k^2 until the first evolve_radius
+    s0.rho0 = q.rho0 > 0 ? q.rho0 : 1.0;
+    s0.istep = 0;
     LAPS_CK(cudaMemcpy(st, &s0, sizeof(s0), cudaMemcpyHostToDevice));
     npart = 4096;
     d_part = dalloc<double>((size_t)npart * 32);
@@ -243,7 +264,7 @@ template <class T> class Engine : public EngineBase {
 
   KTab<T> ktab() const {
     KTab<T> K;
-    K.wx = (const T*)t_wx; K.wy = (const T*)t_wy; K.kyd = (const T*)t_kyd; K.kzd = (const T*)t_kzd;
+    K.wx = (const T*)t_wx; K.kxd = (const T*)t_kxd; K.wy = (const T*)t_wy; K.kyd = (const T*)t_kyd; K.kzd = (const T*)t_kzd;
     K.kx2 = (const T*)t_kx2; K.ky2 = (const T*)t_ky2; K.kz2 = (const T*)t_kz2;
     K.fx = (const T*)t_fx; K.fy = (const T*)t_fy; K.fz = (const T*)t_fz;
     K.kxlim = kxlim;
@@ -251,8 +272,8 @@ template <class T> class Engine : public EngineBase {
   }
 
   void tables() {
-    k_tables<T><<<1, 256, 0, stream>>>(d_wx, d_wy, d_wz, t_wx, t_wy, t_kyd, t_kzd, t_kx2, t_ky2, t_kz2, gfull.nh, p.ny, p.nz,
-                                       p.radius0, st);
+    k_tables<T><<<1, 256, 0, stream>>>(d_wx, d_wy, d_wz, t_wx, t_kxd, t_wy, t_kyd, t_kzd, t_kx2, t_ky2, t_kz2, gfull.nh, p.ny,
+                                       p.nz, p.radius0, P.zrad, st);
     LAPS_CK(cudaGetLastError());
   }
 
@@ -294,7 +315,10 @@ template <class T> class Engine : public EngineBase {
   void passB(const PassArgs& a) { launch_passB<T>(stream, p.ny, B, a, pc, ktab(), twy); }
   void passC(const PassArgs& a) { launch_passC<T>(stream, p.nx, B, a, pc, twx); }
   void passD(const PassArgs& a) { launch_passD<T>(stream, p.ny, B, a, pc, ktab(), twy); }
-  void passE(const PassArgs& a) { launch_passE<T>(stream, p.nz, B, a, pc, ktab(), twz); }
+  void passE(const PassArgs& a) {
+    if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T>(stream, p.nz, B, a, pc, ktab(), twz);
+    else launch_passE<T>(stream, p.nz, B, a, pc, ktab(), twz);
+  }
 
   // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage
   const Geo& g_in() const { return (prune_ok && dealiased) ? gprune : gfull; }
@@ -304,7 +328,7 @@ template <class T> class Engine : public EngineBase {
   void enqueue_stage(int stage, bool cfl, bool store_rk) {
     const Geo& gi = g_in();
     PassArgs ai = args(gi, stage, store_rk, cfl);
-    passA(ai);
+    if (!P.two_d) passA(ai);  // nz = 1: pass B reads the state directly
     mark(0);
     passB(ai);
     mark(1);
@@ -314,7 +338,7 @@ template <class T> class Engine : public EngineBase {
     passC(ac);
     mark(2);
     if (cfl) {
-      k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl);
+      k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl, P.dstep, P.limit_dt, 0);
       LAPS_CK(cudaGetLastError());
       mark(5);
     }
@@ -331,7 +355,7 @@ template <class T> class Engine : public EngineBase {
     enqueue_stage(0, true, true);
     enqueue_stage(1, false, true);
     enqueue_stage(2, false, false);
-    k_advance_time<<<1, 32, 0, stream>>>(st, p.radius0, P.Ur);
+    k_advance_time<<<1, 32, 0, stream>>>(st, p.radius0, P.Ur, P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     tables();
     mark(5);
@@ -410,7 +434,8 @@ template <class T> class Engine : public EngineBase {
     const Geo& g = gfull;
     double* stage = (double*)B.W2;  // 8 real float64 fields fit in 15 complex fields
     LAPS_CK(cudaMemcpyAsync(stage, h, 8 * g.fsr * sizeof(double), cudaMemcpyHostToDevice, stream));
-    k_upload_convert<T><<<1024, 256, 0, stream>>>(stage, (SR*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma);
+    k_upload_convert<T><<<1024, 256, 0, stream>>>(stage, (SR*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma,
+                                                  P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     forward3d((const SR*)B.W1, B.U, 8);
     // mhd.f90:135: dt = 0 before the first vardt, so the first CFL value is taken as is
@@ -435,12 +460,12 @@ template <class T> class Engine : public EngineBase {
     if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
     const Geo& gi = g_in();
     PassArgs a = args(gi, 0, 0, 1);
-    passA(a);
+    if (!P.two_d) passA(a);
     passB(a);
     PassArgs ac = a;
     ac.cfl = 2;  // CFL only: skip the fluxes
     passC(ac);
-    k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl);
+    k_finalize_dt<<<1, 32, 0, stream>>>(st, P.cfl, P.dstep, P.limit_dt, 1);
     LAPS_CK(cudaGetLastError());
     read_state();
     return h_st->dt;
@@ -483,7 +508,7 @@ template <class T> class Engine : public EngineBase {
     inverse3d(B.U, 8);
     double* out = (double*)B.W2;  // 12 real float64 fields fit in 15 complex fields
     k_download_convert<T><<<1024, 256, 0, stream>>>((const SR*)B.W1, uu ? out : nullptr, prim ? out + 8 * g.fsr : nullptr,
-                                                    g.fsr, P.gamma);
+                                                    g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     if (uu) LAPS_CK(cudaMemcpyAsync(uu, out, 8 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
     if (prim) LAPS_CK(cudaMemcpyAsync(prim, out + 8 * g.fsr, 4 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -518,7 +543,7 @@ template <class T> class Engine : public EngineBase {
     i->kx_keep = gprune.kx_keep;
     i->ky_keep = gprune.nky();
     i->kz_keep = gprune.nkz();
-    i->kernels_per_step = 3 * 5 + 3;
+    i->kernels_per_step = 3 * (P.two_d ? 4 : 5) + 3;
     i->graph = graph_steady != nullptr;
   }
 };
@@ -534,7 +559,7 @@ template <class T> void Engine<T>::diagnostics(laps_diag* d) {
   inverse3d(B.U, 8);  // real conserved T fields in W1
   int nb = npart;
   // pass 1: sums of f and f^2 for the 8 reported fields, the energies and u.B
-  k_diag_sums<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, P.gamma, d_part);
+  k_diag_sums<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI, d_part);
   LAPS_CK(cudaGetLastError());
   std::vector<double> part((size_t)nb * 32);
   LAPS_CK(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -569,6 +594,23 @@ template <class T> void Engine<T>::diagnostics(laps_diag* d) {
   for (int k = 0; k < 3; k++) d->rho_u2[k] = r2[k] / n;
   d->max_divB = mx;
   d->h_mag = hm;
+  // real-space maxima of div B and div(rho u)/rho0 (the incompressible code's diagnostics)
+  double mreal[2];
+  for (int w = 0; w < 2; w++) {
+    C* spec = B.W2 + (w2_fields(p) - 1) * g.fsc;
+    k_spec_div<T><<<1024, 256, 0, stream>>>(B.U, spec, g, ktab(), P, pc, st, w == 0 ? 4 : 1, w == 1);
+    LAPS_CK(cudaGetLastError());
+    inverse3d(spec, 1);
+    k_max_abs<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, d_part);
+    LAPS_CK(cudaGetLastError());
+    LAPS_CK(cudaMemcpyAsync(part.data(), d_part, (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
+    double m = 0;
+    for (int b = 0; b < nb; b++) m = std::fmax(m, part[b]);
+    mreal[w] = m;
+  }
+  d->max_divB_real = mreal[0];
+  d->max_divV_real = mreal[1];
 }
 
 }  // namespace laps

@@ -182,7 +182,9 @@ template <class T, int N, int DIR, int JS, int LS>
 __device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t, bool active,
                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
   using P = Plan<N>;
-  if constexpr (N < 16) {
+  if constexpr (N == 1) {  // a length-1 transform is the identity (nz = 1)
+    __syncthreads();
+  } else if constexpr (N < 16) {
     fft_stage<T, N, DIR, N, JS, LS>(s, l, t, active, 1, 0, tw, twstep);
   } else {
     int ns = 1, lns = 0;

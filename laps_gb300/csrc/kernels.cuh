@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(128) k_row_c2r(const typename Store<T>::C* __r
 // primitive (rho, u, B, p) or conserved doubles -> conserved T; mhdinit.f90:1038-1056
 template <class T>
 __global__ void k_upload_convert(const double* __restrict__ h, typename Store<T>::R* __restrict__ u, long long n, int primitive,
-                                 double gamma) {
+                                 double gamma, int incomp) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v[8];
 #pragma unroll
@@ -205,7 +205,8 @@ __global__ void k_upload_convert(const double* __restrict__ h, typename Store<T>
       v[1] = v[0] * ux;
       v[2] = v[0] * uy;
       v[3] = v[0] * uz;
-      v[7] = p / (gamma - 1) + 0.5 * (v[0] * (ux * ux + uy * uy + uz * uz) + v[4] * v[4] + v[5] * v[5] + v[6] * v[6]);
+      // the incompressible state keeps p in slot 8 (src_incompressible/mhdinit.f90:1031-1042)
+      if (!incomp) v[7] = p / (gamma - 1) + 0.5 * (v[0] * (ux * ux + uy * uy + uz * uz) + v[4] * v[4] + v[5] * v[5] + v[6] * v[6]);
     }
 #pragma unroll
     for (int f = 0; f < 8; f++) Store<T>::st(u + f * n + i, Real<T>::from_d(v[f]));
@@ -215,7 +216,7 @@ __global__ void k_upload_convert(const double* __restrict__ h, typename Store<T>
 // conserved T -> conserved doubles + primitives (ux, uy, uz, p); mhdrhs.f90:282-294
 template <class T>
 __global__ void k_download_convert(const typename Store<T>::R* __restrict__ u, double* __restrict__ h, double* __restrict__ hp,
-                                   long long n, double gamma) {
+                                   long long n, double gamma, int incomp) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v[8];
 #pragma unroll
@@ -229,7 +230,7 @@ __global__ void k_download_convert(const typename Store<T>::R* __restrict__ u, d
       hp[0 * n + i] = ux;
       hp[1 * n + i] = uy;
       hp[2 * n + i] = uz;
-      hp[3 * n + i] = (v[7] - 0.5 * (v[1] * ux + v[2] * uy + v[3] * uz + v[4] * v[4] + v[5] * v[5] + v[6] * v[6])) * (gamma - 1);
+      hp[3 * n + i] = incomp ? v[7] : (v[7] - 0.5 * (v[1] * ux + v[2] * uy + v[3] * uz + v[4] * v[4] + v[5] * v[5] + v[6] * v[6])) * (gamma - 1);
     }
   }
 }
@@ -265,15 +266,17 @@ __global__ void k_spec_from_ref(const double2* __restrict__ in, typename Store<T
 // AEBmod.f90:56-73,87-125; derivative factors of mhdrhs.f90:191-204).
 template <class T>
 __global__ void k_tables(const double* __restrict__ wxd, const double* __restrict__ wyd, const double* __restrict__ wzd,
-                         typename Store<T>::R* wx, typename Store<T>::R* wy, typename Store<T>::R* kyd,
+                         typename Store<T>::R* wx, typename Store<T>::R* kxd, typename Store<T>::R* wy, typename Store<T>::R* kyd,
                          typename Store<T>::R* kzd, typename Store<T>::R* kx2, typename Store<T>::R* ky2,
-                         typename Store<T>::R* kz2, int nh, int ny, int nz, double R0, const StepState* st) {
+                         typename Store<T>::R* kz2, int nh, int ny, int nz, double R0, int zrad, const StepState* st) {
   double R = st->radius;
   int plain = st->ksq_plain;
   for (int i = threadIdx.x; i < nh; i += blockDim.x) {
     double k = wxd[i];
+    double kd = zrad ? k * R0 / R : k;  // src_compressible/2D/mhdrhs.f90:278-280
     Store<T>::st(wx + i, Real<T>::from_d(k));
-    Store<T>::st(kx2 + i, Real<T>::from_d(k * k));
+    Store<T>::st(kxd + i, Real<T>::from_d(kd));
+    Store<T>::st(kx2 + i, Real<T>::from_d(plain ? k * k : kd * kd));
   }
   for (int i = threadIdx.x; i < ny; i += blockDim.x) {
     double k = wyd[i];
@@ -292,14 +295,21 @@ __global__ void k_tables(const double* __restrict__ wxd, const double* __restric
 
 // vardt tail: dt = cfl * min, kept within +-2 %, floor check, rkt_init coefficients
 // (mhd.f90:418-428, rktmod.f90:15-27).
-static __global__ void k_finalize_dt(StepState* st, double cfl) {
+// The 2-D code recomputes dt only every dstep steps and may forbid increases
+// (src_compressible/2D/mhd.f90:237-240,396-405).  force: an explicit laps_vardt call.
+static __global__ void k_finalize_dt(StepState* st, double cfl, int dstep, int limit_dt, int force) {
   if (threadIdx.x | blockIdx.x) return;
   if (st->halt) return;
   double m = __longlong_as_double((long long)st->cfl_bits);
   st->cfl_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
+  if (!force && dstep > 1 && st->istep % dstep != 0) return;
   double dtmin = m * cfl;
   double dt = st->dt;
-  if (dt < 0.98 * dtmin || dt > 1.02 * dtmin) dt = dtmin;
+  if (limit_dt) {
+    if (dt == 0.0 || dt > 1.02 * dtmin) dt = dtmin;
+  } else if (dt < 0.98 * dtmin || dt > 1.02 * dtmin) {
+    dt = dtmin;
+  }
   st->dt = dt;
   st->cc[0] = 8.0 / 15.0 * dt; st->ddc[0] = 0.0;
   st->cc[1] = 5.0 / 12.0 * dt; st->ddc[1] = -17.0 / 60.0 * dt;
@@ -313,10 +323,16 @@ static __global__ void k_finalize_dt(StepState* st, double cfl) {
   }
 }
 
-// time += dt; R = R0 + Ur t; tau = R/Ur (mhd.f90:246-248, AEBmod.f90:46-73)
-static __global__ void k_advance_time(StepState* st, double R0, double Ur) {
+// update_rho_p (3-D incompressible, src_incompressible/AEBmod.f90:123-134, at the step's
+// start radius); time += dt; R = R0 + Ur t; tau = R/Ur (mhd.f90:246-248, AEBmod.f90:46-73)
+static __global__ void k_advance_time(StepState* st, double R0, double Ur, int incomp) {
   if (threadIdx.x | blockIdx.x) return;
   if (st->halt) return;
+  if (incomp) {
+    double f = R0 / st->radius;
+    st->rho0 = st->rho0 * (f * f);
+  }
+  st->istep = st->istep + 1;
   st->time = st->time + st->dt;
   st->radius = R0 + Ur * st->time;
   st->inv_tau = Ur != 0.0 ? 1.0 / (st->radius / Ur) : 0.0;

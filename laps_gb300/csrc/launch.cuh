@@ -20,8 +20,8 @@ struct Error {
     if (e_ != cudaSuccess) throw Error{LAPS_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
   } while (0)
 
-#define LAPS_COL_SIZES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512)
-#define LAPS_ROW_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512)
+#define LAPS_COL_SIZES(X) X(1) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
+#define LAPS_ROW_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
 
 template <class K> inline void set_smem(K kernel, int bytes) {
   if (bytes > 48 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -39,8 +39,19 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
                      const typename Store<T>::C* twx);
 template <class T> void launch_passA(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
 template <class T> void launch_passB(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
-template <class T> void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw);
+template <class T, int INCOMP, int CFL>
+void launch_passC_v(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw);
+template <class T> void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
+  if (a.P.variant == LAPS_VARIANT_3DI) {
+    if (a.cfl) launch_passC_v<T, 1, 1>(stream, N, B, a, pc, tw);
+    else launch_passC_v<T, 1, 0>(stream, N, B, a, pc, tw);
+  } else {
+    if (a.cfl) launch_passC_v<T, 0, 1>(stream, N, B, a, pc, tw);
+    else launch_passC_v<T, 0, 0>(stream, N, B, a, pc, tw);
+  }
+}
 template <class T> void launch_passD(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
 template <class T> void launch_passE(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+template <class T> void launch_passE3i(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
 
 }  // namespace laps

@@ -65,7 +65,8 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passA<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, a.hall ? 10 : 8);                    \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE,                                     \
+              a.P.variant == LAPS_VARIANT_3DI ? 12 : (a.hall ? 10 : 8));                                                \
     k_passA<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
     break;                                                                                                              \
   }
@@ -75,7 +76,8 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passB<T, NN>, CL::SMEM);                                                                                 \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.hall ? 11 : 8);                       \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
+              a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
     k_passB<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
     break;                                                                                                              \
   }
@@ -85,7 +87,7 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passD<T, NN>, 2 * CL::SMEM);                                                                             \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, 12);                                    \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : 12); \
     k_passD<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
     break;                                                                                                              \
   }
@@ -101,21 +103,28 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
   }
 LAPS_COL_PASS(launch_passE, k_passE, nky)
 #undef LAPS_CASE
+#define LAPS_CASE(NN)                                                                                                   \
+  case NN: {                                                                                                            \
+    using CL = Col<T, NN>;                                                                                              \
+    set_smem(k_passE3i<T, NN>, 3 * CL::SMEM);                                                                           \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, 4);                                  \
+    k_passE3i<T, NN><<<grid, CL::THREADS, 3 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                     \
+    break;                                                                                                              \
+  }
+LAPS_COL_PASS(launch_passE3i, k_passE3i, nky)
+#undef LAPS_CASE
 #undef LAPS_COL_PASS
 
-template <class T>
-void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
+// pass C for one (physics, CFL) combination; each combination is instantiated in its own
+// translation unit (launch_passC_<type>_<c|i><0|1>.cu)
+template <class T, int INCOMP, int CFL>
+void launch_passC_v(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CF = PassCCfg<NN>;                                                                                            \
     unsigned nb = (unsigned)((long long)a.g.ny * a.g.nz / CF::ROWS);                                                    \
-    if (a.cfl) {                                                                                                        \
-      set_smem(k_passC<T, NN, 1>, CF::SMEM);                                                                            \
-      k_passC<T, NN, 1><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                           \
-    } else {                                                                                                            \
-      set_smem(k_passC<T, NN, 0>, CF::SMEM);                                                                            \
-      k_passC<T, NN, 0><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                           \
-    }                                                                                                                   \
+    set_smem(k_passC<T, NN, CFL, INCOMP>, CF::SMEM);                                                                    \
+    k_passC<T, NN, CFL, INCOMP><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                   \
     break;                                                                                                              \
   }
   switch (N) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }

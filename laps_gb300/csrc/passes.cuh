@@ -4,6 +4,7 @@
 // tile (TX adjacent columns) of one field group, so each CTA runs 1-3 FFTs and keeps
 // partial results in shared-memory buffers, not registers.
 #pragma once
+#include <type_traits>
 #include "kernels.cuh"
 
 namespace laps {
@@ -37,9 +38,15 @@ template <class T, int N, int NBUF> struct ColCtx {
 };
 
 // ============================================================================ pass A
-// inverse z-FFT of state field f = blockIdx.z (0..7), or for the Hall current
-// f = 8: C_x = IFFT_z(-i kz B_y), f = 9: C_y = IFFT_z(i kz B_x).
-// Tile: kx0..kx0+7, one kept ky row; writes all z of W1.
+// inverse z-FFT of output f = blockIdx.z: state field src[f], optionally times -i kz or +i kz:
+//   compressible:   0..7 state, 8: C_x = IFFT_z(-i kz B_y), 9: C_y = IFFT_z(i kz B_x) (Hall)
+//   incompressible: 0..6 state, 7: C_x, 8: C_y, 9..11: IFFT_z(i kz (rho u)_c), c = x, y, z
+// Tile: kx0..kx0+7, one kept ky row; writes all z of W1.  (Not used in 2-D: nz = 1.)
+struct ATab { signed char src, mult; };
+__constant__ ATab c_atab[2][12] = {
+    {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {7, 0}, {5, -1}, {4, 1}, {0, 0}, {0, 0}},
+    {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {5, -1}, {4, 1}, {1, 1}, {2, 1}, {3, 1}}};
+
 template <class T, int NZ>
 __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
   using CL = Col<T, NZ>;
@@ -49,22 +56,22 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T> b, PassAr
   ColCtx<T, NZ, 1> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
   const int f = blockIdx.z;
+  const ATab e = c_atab[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][f];
   int kx = blockIdx.x * TX + x.c;
   int r = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && r < g.nky();
   int ky = ok ? g.ky_of(r) : 0;
   long long col = (long long)ky * g.kxp + kx;  // + z * ny * kxp
   long long zs = (long long)g.ny * g.kxp;
-  const int src = f < 8 ? f : (f == 8 ? 5 : 4);
-  const C* in = b.U + src * g.fsc + col;
+  const C* in = b.U + e.src * g.fsc + col;
 #pragma unroll 4
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.kz_in(kz)) {
       v = Store<T>::ldg(in + kz * zs);
-      if (f == 8) v = -mul_i(v, K.kzd[kz]);
-      else if (f == 9) v = mul_i(v, K.kzd[kz]);
+      if (e.mult < 0) v = -mul_i(v, K.kzd[kz]);
+      else if (e.mult > 0) v = mul_i(v, K.kzd[kz]);
     }
     Store<T>::stc(x.at(0, m), v);
   }
@@ -77,9 +84,37 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T> b, PassAr
 }
 
 // ============================================================================ pass B
-// inverse y-FFT of field f = blockIdx.z: the 8 state fields, and for the Hall current
-//   8: Jx = i ay W1[Bz] + W1[Cx],  9: Jy = W1[Cy] - i ax W1[Bz],  10: Jz = i ax W1[By] - i ay W1[Bx]
+// inverse y-FFT of output f = blockIdx.z, the sum of up to two input columns each times
+// 1, i ax or i ay (signed):
+//   compressible 3-D: 0..7 state; J: 8 = i ay W1[Bz] + W1[Cx], 9 = W1[Cy] - i ax W1[Bz],
+//                     10 = i ax W1[By] - i ay W1[Bx]
+//   compressible 2-D: the same reading the state U directly (nz = 1, kz = 0: no C terms)
+//   incompressible:   0..6 state; J: 7, 8, 9; grad(rho u): 10 + 3c + d = d/dx_d (rho u)_c
 // Tile: kx0..kx0+7, one z plane; reads kept ky rows, writes all y of W2.
+enum { BF_ONE = 1, BF_AX = 2, BF_MAX = -2, BF_AY = 3, BF_MAY = -3 };
+struct BTab { signed char in0, f0, in1, f1; };
+__constant__ BTab c_btab[3][19] = {
+    {{0, 1, -1, 0}, {1, 1, -1, 0}, {2, 1, -1, 0}, {3, 1, -1, 0}, {4, 1, -1, 0}, {5, 1, -1, 0}, {6, 1, -1, 0}, {7, 1, -1, 0},
+     {6, BF_AY, 8, BF_ONE}, {9, BF_ONE, 6, BF_MAX}, {5, BF_AX, 4, BF_MAY}},
+    {{0, 1, -1, 0}, {1, 1, -1, 0}, {2, 1, -1, 0}, {3, 1, -1, 0}, {4, 1, -1, 0}, {5, 1, -1, 0}, {6, 1, -1, 0}, {7, 1, -1, 0},
+     {6, BF_AY, -1, 0}, {6, BF_MAX, -1, 0}, {5, BF_AX, 4, BF_MAY}},
+    {{0, 1, -1, 0}, {1, 1, -1, 0}, {2, 1, -1, 0}, {3, 1, -1, 0}, {4, 1, -1, 0}, {5, 1, -1, 0}, {6, 1, -1, 0},
+     {6, BF_AY, 7, BF_ONE}, {8, BF_ONE, 6, BF_MAX}, {5, BF_AX, 4, BF_MAY},
+     {1, BF_AX, -1, 0}, {1, BF_AY, -1, 0}, {9, BF_ONE, -1, 0},
+     {2, BF_AX, -1, 0}, {2, BF_AY, -1, 0}, {10, BF_ONE, -1, 0},
+     {3, BF_AX, -1, 0}, {3, BF_AY, -1, 0}, {11, BF_ONE, -1, 0}}};
+
+template <class T>
+__device__ __forceinline__ cx<T> bterm(cx<T> v, int f, T ax, T ay) {
+  switch (f) {
+    case BF_AX: return mul_i(v, ax);
+    case BF_MAX: return -mul_i(v, ax);
+    case BF_AY: return mul_i(v, ay);
+    case BF_MAY: return -mul_i(v, ay);
+    default: return v;
+  }
+}
+
 template <class T, int NY>
 __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twy) {
   using CL = Col<T, NY>;
@@ -89,26 +124,25 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassAr
   ColCtx<T, NY, 1> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
   const int f = blockIdx.z;
+  const int vt = a.P.variant == LAPS_VARIANT_3DI ? 2 : (a.P.two_d ? 1 : 0);
+  const BTab e = c_btab[vt][f];
+  const C* src = a.P.two_d ? b.U : b.W1;
   int kx = blockIdx.x * TX + x.c;
   int z = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && z < g.nz;
   long long col = (long long)z * g.ny * g.kxp + kx;  // + y * kxp
   T rr = Real<T>::from_d(a.st->r_ratio);
+  const bool kf = e.f0 > 1 || e.f0 < 0 || e.f1 > 1 || e.f1 < 0;
 #pragma unroll 4
   for (int m = 0; m < CL::EPT; m++) {
     int ky = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.ky_in(ky)) {
-      const C* w = b.W1 + col + (long long)ky * g.kxp;
-      if (f < 8) {
-        v = Store<T>::ldg(w + f * g.fsc);
-      } else {
-        T ax, ay, az;
-        kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
-        if (f == 8) v = mul_i(Store<T>::ldg(w + 6 * g.fsc), ay) + Store<T>::ldg(w + 8 * g.fsc);
-        else if (f == 9) v = Store<T>::ldg(w + 9 * g.fsc) - mul_i(Store<T>::ldg(w + 6 * g.fsc), ax);
-        else v = mul_i(Store<T>::ldg(w + 5 * g.fsc), ax) - mul_i(Store<T>::ldg(w + 4 * g.fsc), ay);
-      }
+      const C* w = src + col + (long long)ky * g.kxp;
+      T ax = pc.zero, ay = pc.zero, az;
+      if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+      v = bterm(Store<T>::ldg(w + e.in0 * g.fsc), e.f0, ax, ay);
+      if (e.in1 >= 0) v = v + bterm(Store<T>::ldg(w + e.in1 * g.fsc), e.f1, ax, ay);
     }
     Store<T>::stc(x.at(0, m), v);
   }
@@ -121,15 +155,19 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassAr
 }
 
 // ============================================================================ pass C
-// Per x-row (y, z): c2r of the 8 (+3) fields, the real-space fluxes of calc_flux
-// (mhdrhs.f90:21-124, with the primitives of update_uu_prim_from_uu, :282-294), the CFL
-// minimum of vardt (mhd.f90:350-416) when asked, and r2c of the 18 (+1) fluxes.
+// Per x-row (y, z): c2r of the inputs, the real-space physics, the CFL minimum of vardt when
+// asked, and r2c of the outputs.
+//   compressible (Flux): calc_flux (mhdrhs.f90:21-124, 2D/mhdrhs.f90:23-132) with the
+//     primitives of update_uu_prim_from_uu (:282-294); 11 inputs (8 state + J), 18 (+1) outputs
+//   incompressible (FluxI): calc_flux_for_pressure and calc_flux
+//     (src_incompressible/mhdrhs.f90:25-84,393-437); 19 inputs (7 state, J, grad(rho u)),
+//     6 outputs (pressure flux, E)
 template <class T>
 struct Flux {
   // in: rho, mx, my, mz, Bx, By, Bz, e, Jx, Jy, Jz ; out(k, value) receives the 18 fluxes and
   // the expansion term (k = 18) one at a time, so that they need not all be live at once
   template <class OUT>
-  __device__ __forceinline__ static void eval(const T* q, OUT out, const PT<T>& c, int hall, int aeb, T inv_tau) {
+  __device__ __forceinline__ static void eval(const T* q, OUT out, const PT<T>& c, const Phys& P, T inv_tau, T inv_rho0) {
     const T half = c.half, gm1 = c.gm1;
     const T rho = q[0], mx = q[1], my = q[2], mz = q[3], Bx = q[4], By = q[5], Bz = q[6], e = q[7];
     const T rinv = c.one / rho;
@@ -150,7 +188,7 @@ struct Flux {
     out(10, my * uz - By * Bz);
     out(11, mz * uz - Bz * Bz + ptot);
     T ex = uz * By - uy * Bz, ey = ux * Bz - uz * Bx, ez = uy * Bx - ux * By;
-    if (hall) {
+    if (P.hall) {
       const T dr = c.di * rinv;
       const T Jx = q[8], Jy = q[9], Jz = q[10];
       ex = ex + dr * (Jy * Bz - Jz * By);
@@ -165,13 +203,17 @@ struct Flux {
     out(15, ep * ux - udotb * Bx);
     out(16, ep * uy - udotb * By);
     out(17, ep * uz - udotb * Bz);
-    if (aeb) {
+    if (P.aeb) {
       const T two = c.two;
-      out(18, c.cg * p * inv_tau - (two * Bx * Bx + By * By + Bz * Bz) * inv_tau - (mx * ux + two * my * uy + two * mz * uz) * inv_tau);
+      if (P.zrad)  // 2D/mhdrhs.f90:96-100
+        out(18, c.cg * p * inv_tau - (Bx * Bx + By * By + two * Bz * Bz) * inv_tau - (two * mx * ux + two * my * uy + mz * uz) * inv_tau);
+      else
+        out(18, c.cg * p * inv_tau - (two * Bx * Bx + By * By + Bz * Bz) * inv_tau - (mx * ux + two * my * uy + two * mz * uz) * inv_tau);
     }
   }
-  // min over the three axes of dx_i / c_max,i (mhd.f90:355-409)
-  __device__ __forceinline__ static T cfl(const T* q, const PT<T>& c, int hall, T rfac) {
+  // min over the axes of dx_i / c_max,i (mhd.f90:355-409; 2-D: x and y only, the
+  // explicit-resistivity term and radial x, 2D/mhd.f90:313-392)
+  __device__ __forceinline__ static T cfl(const T* q, const PT<T>& c, const Phys& P, T rfac) {
     const T zero = c.zero, four = c.four, half = c.half;
     const T is2 = c.is2;
     T rho = q[0], rinv = c.one / rho;
@@ -185,8 +227,10 @@ struct Flux {
     T ca2 = ca[0] * ca[0] + ca[1] * ca[1] + ca[2] * ca[2];
     T cms2 = cs2 + ca2;
     T cmax[3];
+    const int nd = P.two_d ? 2 : 3;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
+      if (d >= nd) { cmax[d] = c.one; continue; }
       T cns = Real<T>::sqrt_(Real<T>::max_(cms2 * cms2 - (four * cs2) * (ca[d] * ca[d]), zero));
       T cf = Real<T>::sqrt_(cms2 + cns) * is2;
       T cs = Real<T>::sqrt_(Real<T>::max_(cms2 - cns, zero)) * is2;
@@ -199,8 +243,68 @@ struct Flux {
       m = Real<T>::max_(m, Real<T>::abs_(u[d]));
       cmax[d] = m;
     }
-    if (hall) {
+    if (P.two_d && P.resis && P.resis_exp) {
+      cmax[0] = Real<T>::max_(cmax[0], c.eta_dx);
+      cmax[1] = Real<T>::max_(cmax[1], c.eta_dy);
+    }
+    if (P.hall) {
       T bm = Real<T>::max_(Real<T>::max_(Bx, By), Bz);
+      T ch = c.di * rinv * bm * c.inv_mindx;
+#pragma unroll
+      for (int d = 0; d < 3; d++) cmax[d] = Real<T>::max_(cmax[d], ch);
+    }
+    T dtx = c.dx / cmax[0];
+    if (P.zrad) dtx = dtx * rfac;
+    T dty = c.dy / cmax[1] * rfac;
+    if (P.two_d) return Real<T>::min_(dtx, dty);
+    T dtz = c.dz / cmax[2] * rfac;
+    return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
+  }
+};
+
+template <class T>
+struct FluxI {
+  // in: rho, mx, my, mz, Bx, By, Bz, Jx, Jy, Jz, then d/dx_d (rho u)_c at 10 + 3c + d
+  // (times 1/rho0 here); out: pressure flux fp (0..2) and the electric field (3..5)
+  template <class OUT>
+  __device__ __forceinline__ static void eval(const T* q, OUT out, const PT<T>& c, const Phys& P, T inv_tau, T inv_rho0) {
+    const T rho = q[0], mx = q[1], my = q[2], mz = q[3], Bx = q[4], By = q[5], Bz = q[6];
+    const T Jx = q[7], Jy = q[8], Jz = q[9];
+    T g[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) g[i] = q[10 + i] * inv_rho0;
+    out(0, -mx * g[0] - my * g[1] - mz * g[2] + Jy * Bz - Jz * By);
+    out(1, -mx * g[3] - my * g[4] - mz * g[5] + Jz * Bx - Jx * Bz);
+    out(2, -mx * g[6] - my * g[7] - mz * g[8] + Jx * By - Jy * Bx);
+    const T rinv = c.one / rho;
+    const T ux = mx * rinv, uy = my * rinv, uz = mz * rinv;
+    T ex = uz * By - uy * Bz, ey = ux * Bz - uz * Bx, ez = uy * Bx - ux * By;
+    if (P.hall) {
+      const T dr = c.di * rinv;
+      ex = ex + dr * (Jy * Bz - Jz * By);
+      ey = ey + dr * (Jz * Bx - Jx * Bz);
+      ez = ez + dr * (Jx * By - Jy * Bx);
+    }
+    out(3, ex);
+    out(4, ey);
+    out(5, ez);
+  }
+  // Alfven-only CFL (src_incompressible/mhd.f90:394-463)
+  __device__ __forceinline__ static T cfl(const T* q, const PT<T>& c, const Phys& P, T rfac) {
+    T rho = q[0], rinv = c.one / rho;
+    T u[3] = {q[1] * rinv, q[2] * rinv, q[3] * rinv};
+    T sq = Real<T>::sqrt_(rho);
+    T cmax[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      T ca = q[4 + d] / sq;
+      T m = Real<T>::abs_(u[d] + ca);
+      m = Real<T>::max_(m, Real<T>::abs_(u[d] - ca));
+      m = Real<T>::max_(m, Real<T>::abs_(u[d]));
+      cmax[d] = m;
+    }
+    if (P.hall) {
+      T bm = Real<T>::max_(Real<T>::max_(q[4], q[5]), q[6]);
       T ch = c.di * rinv * bm * c.inv_mindx;
 #pragma unroll
       for (int d = 0; d < 3; d++) cmax[d] = Real<T>::max_(cmax[d], ch);
@@ -211,7 +315,6 @@ struct Flux {
     return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
   }
 };
-
 
 // rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
 // (Hall) in one batch and their 38 outputs in two
@@ -227,7 +330,7 @@ template <int NX> struct PassCCfg {
   static constexpr int SMEM = ROWS * NF * LC * 16;
 };
 
-template <class T, int NX, int CFL>
+template <class T, int NX, int CFL, int INCOMP>
 __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, PassArgs a, PT<T> pc, const typename Store<T>::C* __restrict__ twx) {
   using CF = PassCCfg<NX>;
   using C = typename Store<T>::C;
@@ -238,8 +341,8 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   C* sc = reinterpret_cast<C*>(smem_raw);  // [row][field] lines of LC complex
   SR* sr = reinterpret_cast<SR*>(smem_raw);
   const Geo& g = a.g;
-  const int nin = a.hall ? 11 : 8;
-  const int nfl = a.cfl == 2 ? 0 : (a.aeb ? 19 : 18);  // a.cfl == 2: CFL minimum only
+  const int nin = INCOMP ? 19 : (a.hall ? 11 : 8);
+  const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.aeb ? 19 : 18));  // a.cfl == 2: CFL minimum only
   long long row0 = (long long)blockIdx.x * CF::ROWS;  // row = z*ny + y
   const int lt = threadIdx.x % CF::TPL, lb = threadIdx.x / CF::TPL;
   // ---- c2r of the inputs
@@ -261,19 +364,22 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   bool nan_seen = false;
   const T rfac = Real<T>::from_d(a.st->radius / a.P.R0);
   const T inv_tau = Real<T>::from_d(a.st->inv_tau);
+  const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
 #pragma unroll 1
   for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
     int rr = p / NX, xx = row_real_idx(p % NX);
     SR* base = sr + 2 * rr * CF::NF * CF::LC + xx;
-    T q[11];
+    constexpr int NQ = INCOMP ? 19 : 11;
+    T q[NQ];
 #pragma unroll
-    for (int f = 0; f < 11; f++) q[f] = f < nin ? Store<T>::ld(base + 2 * f * CF::LC) : pc.zero;
+    for (int f = 0; f < NQ; f++) q[f] = f < nin ? Store<T>::ld(base + 2 * f * CF::LC) : pc.zero;
+    using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
     if (CFL) {
-      T d = Flux<T>::cfl(q, pc, a.hall, rfac);
+      T d = PH::cfl(q, pc, a.P, rfac);
       if (Real<T>::isnan_(d)) nan_seen = true;
       else tmin = Real<T>::min_(tmin, d);
     }
-    if (nfl > 0) Flux<T>::eval(q, [&](int k, T v) { Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.hall, a.aeb, inv_tau);
+    if (nfl > 0) PH::eval(q, [&](int k, T v) { Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   if (CFL) {
     double dmin = Real<T>::to_d(tmin);
@@ -306,21 +412,25 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
 
 // ============================================================================ pass D
 // forward y-FFT of the fluxes with the kx, ky parts of the spectral right-hand side folded
-// in (calc_rhs, mhdrhs.f90:206-233), leaving only the kz parts for pass E.  Output slots:
+// in (calc_rhs, mhdrhs.f90:206-233), leaving only the kz parts for pass E.  Compressible
+// output slots:
 //   0 Q1 = -(i ax F1 + i ay F2)      1 F3
 //   2 Q2 = -(i ax F4 + i ay F5)      3 F6
 //   4 Q3 = -(i ax F7 + i ay F8)      5 F9
 //   6 Q4 = -(i ax F10 + i ay F11)    7 F12
 //   8 Ex   9 Ey   10 P7 = i ay Ex - i ax Ey   11 P5 = -i ay Ez   12 P6 = i ax Ez
 //   13 Q8 = -(i ax F16 + i ay F17) + Expand   14 F18
-// One group per blockIdx.z (12 groups); tile: kx0..kx0+7, one z plane; reads all y of W1,
-// writes kept ky rows of W2.
+// Incompressible output slots: 0..2 the pressure flux, 3 Ex, 4 Ey, 5 P7, 6 P5, 7 P6.
+// One group per blockIdx.z; tile: kx0..kx0+7, one z plane; reads all y of W1, writes kept
+// ky rows of W2.
 struct DGroup { signed char in[3], kind, out; };
 enum { DG_Q = 0, DG_COPY, DG_EXY, DG_EZ, DG_Q8 };
-__constant__ DGroup c_dgroups[12] = {
-    {{0, 1, -1}, DG_Q, 0},  {{2, -1, -1}, DG_COPY, 1},  {{3, 4, -1}, DG_Q, 2},    {{5, -1, -1}, DG_COPY, 3},
-    {{6, 7, -1}, DG_Q, 4},  {{8, -1, -1}, DG_COPY, 5},  {{9, 10, -1}, DG_Q, 6},   {{11, -1, -1}, DG_COPY, 7},
-    {{12, 13, -1}, DG_EXY, 8}, {{14, -1, -1}, DG_EZ, 11}, {{15, 16, 18}, DG_Q8, 13}, {{17, -1, -1}, DG_COPY, 14}};
+__constant__ DGroup c_dgroups[2][12] = {
+    {{{0, 1, -1}, DG_Q, 0},  {{2, -1, -1}, DG_COPY, 1},  {{3, 4, -1}, DG_Q, 2},    {{5, -1, -1}, DG_COPY, 3},
+     {{6, 7, -1}, DG_Q, 4},  {{8, -1, -1}, DG_COPY, 5},  {{9, 10, -1}, DG_Q, 6},   {{11, -1, -1}, DG_COPY, 7},
+     {{12, 13, -1}, DG_EXY, 8}, {{14, -1, -1}, DG_EZ, 11}, {{15, 16, 18}, DG_Q8, 13}, {{17, -1, -1}, DG_COPY, 14}},
+    {{{0, -1, -1}, DG_COPY, 0}, {{1, -1, -1}, DG_COPY, 1}, {{2, -1, -1}, DG_COPY, 2}, {{3, 4, -1}, DG_EXY, 3},
+     {{5, -1, -1}, DG_EZ, 6}}};
 
 template <class T, int NY>
 __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twy) {
@@ -330,7 +440,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
   if (a.st->halt) return;
   ColCtx<T, NY, 2> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
-  const DGroup grp = c_dgroups[blockIdx.z];
+  const DGroup grp = c_dgroups[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][blockIdx.z];
   int kx = blockIdx.x * TX + x.c;
   int z = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && z < g.nz;
@@ -350,12 +460,14 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
     __syncthreads();
     fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
     if (grp.kind == DG_Q8 && k == 1) {  // fold the first two into buffer 0 before the third
+      if (ok) {  // padding columns (kx >= nx/2+1) have no wave numbers
 #pragma unroll 2
-      for (int m = 0; m < CL::EPT; m++) {
-        T ax, ay, az;
-        kfac(K, a.P, pc, rr, kx, x.j(m), 0, ax, ay, az);
-        cx<T> q = -(mul_i(Store<T>::ldc(x.at(0, m)), ax) + mul_i(Store<T>::ldc(x.at(1, m)), ay));
-        Store<T>::stc(x.at(0, m), q);
+        for (int m = 0; m < CL::EPT; m++) {
+          T ax, ay, az;
+          kfac(K, a.P, pc, rr, kx, x.j(m), 0, ax, ay, az);
+          cx<T> q = -(mul_i(Store<T>::ldc(x.at(0, m)), ax) + mul_i(Store<T>::ldc(x.at(1, m)), ay));
+          Store<T>::stc(x.at(0, m), q);
+        }
       }
       __syncthreads();
     }
@@ -374,32 +486,86 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
       v1 = Store<T>::ldc(x.at(1, m));
       v1 = {Real<T>::mul_pow2(v1.re, sexp), Real<T>::mul_pow2(v1.im, sexp)};
     }
-    C* o = b.W2 + col + (long long)ky * g.kxp;
+    C* o = b.W2 + col + (long long)ky * g.kxp + grp.out * g.fsc;
     switch (grp.kind) {
-      case DG_Q: Store<T>::stc(o + grp.out * g.fsc, -(mul_i(v0, ax) + mul_i(v1, ay))); break;
-      case DG_COPY: Store<T>::stc(o + grp.out * g.fsc, v0); break;
+      case DG_Q: Store<T>::stc(o, -(mul_i(v0, ax) + mul_i(v1, ay))); break;
+      case DG_COPY: Store<T>::stc(o, v0); break;
       case DG_EXY:
-        Store<T>::stc(o + 8 * g.fsc, v0);
-        Store<T>::stc(o + 9 * g.fsc, v1);
-        Store<T>::stc(o + 10 * g.fsc, mul_i(v0, ay) - mul_i(v1, ax));
+        Store<T>::stc(o, v0);
+        Store<T>::stc(o + g.fsc, v1);
+        Store<T>::stc(o + 2 * g.fsc, mul_i(v0, ay) - mul_i(v1, ax));
         break;
       case DG_EZ:
-        Store<T>::stc(o + 11 * g.fsc, -mul_i(v0, ay));
-        Store<T>::stc(o + 12 * g.fsc, mul_i(v0, ax));
+        Store<T>::stc(o, -mul_i(v0, ay));
+        Store<T>::stc(o + g.fsc, mul_i(v0, ax));
         break;
       default:  // DG_Q8: buffer 0 holds the folded -(i ax F16 + i ay F17), buffer 1 the expansion term
-        Store<T>::stc(o + 13 * g.fsc, nin == 3 ? v0 + v1 : v0);
+        Store<T>::stc(o, nin == 3 ? v0 + v1 : v0);
         break;
     }
   }
 }
 
 // ============================================================================ pass E
-// forward z-FFT with the kz parts of the right-hand side, then for variable v = blockIdx.z:
-// the expansion damping (mhdrhs.f90:235-251), explicit diffusion (:253-275), the RK3 update
-// with implicit diffusion (rktmod.f90:34-62) and the dealias mask or filter
-// (dealiasing.f90:70-113).  Tile: kx0..kx0+7, one kept ky row; reads all z of W2, writes
-// kept kz of U (and R).
+// Per-element tail of the spectral right-hand side and the time advance of variable v:
+// expansion damping (mhdrhs.f90:235-251), explicit diffusion (:253-275), the RK3 update with
+// implicit diffusion (rktmod.f90:34-62) and the dealias mask or filter (dealiasing.f90:70-113).
+template <class T>
+struct RkCtx {
+  const Geo* g;
+  const Phys* P;
+  const PT<T>* pc;
+  const KTab<T>* K;
+  T cc, ddc, ts, inv_tau, rr;
+  int stage, store_rk, plain;
+  __device__ __forceinline__ T k2(int kx, int ky, int kz) const {
+    if (P->corot && !plain) return ksq(*K, *P, *pc, rr, kx, ky, kz);
+    return (K->kx2[kx] + K->ky2[ky]) + K->kz2[kz];
+  }
+  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, typename Store<T>::C* U, typename Store<T>::C* R, T k2,
+                                         int kx, int ky, int kz) const {
+    const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
+    if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - u * (pc->ebm[v] * inv_tau);
+    if (mom && P->visc && P->visc_exp) fnl = fnl - u * (pc->nu * k2);
+    if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc->eta * k2);
+    cx<T> un = fnl * cc + u;
+    if (stage > 0) un = (fnl * cc + Store<T>::ldg(R) * ddc) + u;
+    if (store_rk) Store<T>::stc(R, fnl);
+    if (mom && P->visc && !P->visc_exp) {
+      T d = ts * k2 * pc->nu + pc->one;
+      un = {un.re / d, un.im / d};
+    }
+    if (mag && P->resis && !P->resis_exp) {
+      T d = ts * k2 * pc->eta + pc->one;
+      un = {un.re / d, un.im / d};
+    }
+    if (P->dealias == 1 || P->dealias == 3) {
+      if (kx >= K->kxlim[kz * g->ny + ky]) un = cx_zero<T>();
+    } else if (P->dealias == 2) {
+      un = ((un * K->fx[kx]) * K->fy[ky]) * K->fz[kz];
+    }
+    Store<T>::stc(U, un);
+  }
+};
+
+template <class T>
+__device__ __forceinline__ RkCtx<T> rk_ctx(const PassArgs& a, const PT<T>& pc, const KTab<T>& K) {
+  RkCtx<T> r;
+  r.g = &a.g; r.P = &a.P; r.pc = &pc; r.K = &K;
+  r.stage = a.stage;
+  r.store_rk = a.store_rk;
+  r.cc = Real<T>::from_d(a.st->cc[a.stage]);
+  r.ddc = Real<T>::from_d(a.st->ddc[a.stage]);
+  r.ts = Real<T>::from_d(a.st->ts[a.stage]);
+  r.inv_tau = Real<T>::from_d(a.st->inv_tau);
+  r.rr = Real<T>::from_d(a.st->r_ratio);
+  r.plain = a.st->ksq_plain;
+  return r;
+}
+
+// Compressible: forward z-FFT with the kz parts of the right-hand side, then the tail and
+// the time advance of variable v = blockIdx.z.  Tile: kx0..kx0+7, one kept ky row; reads all
+// z of W2, writes kept kz of U (and R).
 template <class T, int NZ>
 __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
   using CL = Col<T, NZ>;
@@ -408,7 +574,6 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
   if (a.st->halt) return;
   ColCtx<T, NZ, 2> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
-  const Phys& P = a.P;
   const int v = blockIdx.z;
   int kx = blockIdx.x * TX + x.c;
   int r = blockIdx.y * CL::NTILE + x.tl;
@@ -417,9 +582,10 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
   long long col = (long long)ky * g.kxp + kx;
   long long zs = (long long)g.ny * g.kxp;
   const int sexp = -__ffs(NZ) + 1;
-  // inputs per variable: first (plain), second (times s * i kz), s = +-1 or 0 (none)
+  // inputs per variable: first (plain), second (times s * i kz), s = +-1 or 0 (none; also
+  // in 2-D, where kz = 0)
   const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
-  const int in2 = v == 4 ? 9 : v == 5 ? 8 : v == 6 ? -1 : v == 7 ? 14 : 2 * v + 1;
+  const int in2 = (v == 6 || a.P.two_d) ? -1 : v == 4 ? 9 : v == 5 ? 8 : v == 7 ? 14 : 2 * v + 1;
   const int nin = in2 < 0 ? 1 : 2;
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
@@ -433,14 +599,8 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
     fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
   }
   if (!ok) return;
-  const int stg = a.stage;
-  const T cc = Real<T>::from_d(a.st->cc[stg]), ddc = Real<T>::from_d(a.st->ddc[stg]);
-  const T ts = Real<T>::from_d(a.st->ts[stg]);
-  const T ebmv = pc.ebm[v] * Real<T>::from_d(a.st->inv_tau);
-  const T rr = Real<T>::from_d(a.st->r_ratio);
-  const int plain = a.st->ksq_plain;
-  const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
-  const bool need_k2 = (mom && P.visc) || (mag && P.resis);
+  const RkCtx<T> rk = rk_ctx(a, pc, K);
+  const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
   C* U = b.U + v * g.fsc + col;
   C* R = b.R + v * g.fsc + col;
 #pragma unroll 2
@@ -455,32 +615,86 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
       fnl = v == 4 ? fnl + w : fnl - w;
     }
     long long idx = kz * zs;
-    cx<T> u = Store<T>::ldg(U + idx);
-    T k2 = pc.zero;
-    if (need_k2) {
-      if (P.corot && !plain) k2 = ksq(K, P, pc, rr, kx, ky, kz);
-      else k2 = (K.kx2[kx] + K.ky2[ky]) + K.kz2[kz];
+    T k2 = need_k2 ? rk.k2(kx, ky, kz) : pc.zero;
+    rk.update(v, fnl, Store<T>::ldg(U + idx), U + idx, R + idx, k2, kx, ky, kz);
+  }
+}
+
+// Incompressible (src_incompressible/mhdrhs.f90:117-232,468-518): group blockIdx.z = 0
+// transforms the pressure flux and updates rho, rho u and p:
+//   k.fp = (i k . fp_hat)/k^2, p_hat = -k.fp, fnl(rho u) = fp_hat + k.fp (i k)  (0 where k^2 < 1e-10)
+// groups 1..3 advance Bx, By, Bz from the electric field as in the compressible pass.
+template <class T, int NZ>
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
+  using CL = Col<T, NZ>;
+  using C = typename Store<T>::C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.st->halt) return;
+  ColCtx<T, NZ, 3> x(reinterpret_cast<C*>(smem_raw));
+  const Geo& g = a.g;
+  const int grp = blockIdx.z;
+  int kx = blockIdx.x * TX + x.c;
+  int r = blockIdx.y * CL::NTILE + x.tl;
+  bool ok = kx < g.kx_keep && r < g.nky();
+  int ky = ok ? g.ky_of(r) : 0;
+  long long col = (long long)ky * g.kxp + kx;
+  long long zs = (long long)g.ny * g.kxp;
+  const int sexp = -__ffs(NZ) + 1;
+  // slots: 0..2 fp, 3 Ex, 4 Ey, 5 P7, 6 P5, 7 P6
+  const int nin = grp == 0 ? 3 : (grp == 3 ? 1 : 2);
+  const int ins[4][3] = {{0, 1, 2}, {6, 4, -1}, {7, 3, -1}, {5, -1, -1}};
+#pragma unroll 1
+  for (int k = 0; k < nin; k++) {
+    const C* in = b.W2 + ins[grp][k] * g.fsc + col;
+#pragma unroll 4
+    for (int m = 0; m < CL::EPT; m++) {
+      cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
+      Store<T>::stc(x.at(k, m), w);
     }
-    if (P.aeb && v < 7) fnl = fnl - u * ebmv;
-    if (mom && P.visc && P.visc_exp) fnl = fnl - u * (pc.nu * k2);
-    if (mag && P.resis && P.resis_exp && !(P.cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc.eta * k2);
-    cx<T> un = fnl * cc + u;
-    if (stg > 0) un = (fnl * cc + Store<T>::ldg(R + idx) * ddc) + u;
-    if (a.store_rk) Store<T>::stc(R + idx, fnl);
-    if (mom && P.visc && !P.visc_exp) {
-      T d = ts * k2 * pc.nu + pc.one;
-      un = {un.re / d, un.im / d};
+    __syncthreads();
+    fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
+  }
+  if (!ok) return;
+  const RkCtx<T> rk = rk_ctx(a, pc, K);
+  const T rr = rk.rr;
+#pragma unroll 1
+  for (int m = 0; m < CL::EPT; m++) {
+    int kz = x.j(m);
+    if (!g.kz_in(kz)) continue;
+    long long idx = kz * zs;
+    auto val = [&](int bi) {
+      cx<T> w = Store<T>::ldc(x.at(bi, m));
+      return cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)};
+    };
+    T k2 = rk.k2(kx, ky, kz);
+    if (grp == 0) {
+      T ax, ay, az;
+      kfac(K, a.P, pc, rr, kx, ky, kz, ax, ay, az);
+      cx<T> f0 = val(0), f1 = val(1), f2 = val(2);
+      const bool small = Real<T>::lead(k2) < 1e-10f;
+      cx<T> kdot = cx_zero<T>();
+      if (!small) {
+        cx<T> s = (mul_i(f0, ax) + mul_i(f1, ay)) + mul_i(f2, az);
+        kdot = {s.re / k2, s.im / k2};
+      }
+      const cx<T> fm[3] = {small ? cx_zero<T>() : f0 + mul_i(kdot, ax), small ? cx_zero<T>() : f1 + mul_i(kdot, ay),
+                           small ? cx_zero<T>() : f2 + mul_i(kdot, az)};
+      for (int v = 0; v < 4; v++) {
+        C* U = b.U + v * g.fsc + col + idx;
+        rk.update(v, v == 0 ? cx_zero<T>() : fm[v - 1], Store<T>::ldg(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
+      }
+      C* U = b.U + 7 * g.fsc + col + idx;  // the new pressure replaces slot 8 before the update
+      rk.update(7, cx_zero<T>(), -kdot, U, b.R + 7 * g.fsc + col + idx, k2, kx, ky, kz);
+    } else {
+      const int v = 3 + grp;
+      cx<T> fnl = val(0);
+      if (nin > 1) {
+        cx<T> w = mul_i(val(1), K.kzd[kz]);
+        fnl = v == 4 ? fnl + w : fnl - w;
+      }
+      C* U = b.U + v * g.fsc + col + idx;
+      rk.update(v, fnl, Store<T>::ldg(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
     }
-    if (mag && P.resis && !P.resis_exp) {
-      T d = ts * k2 * pc.eta + pc.one;
-      un = {un.re / d, un.im / d};
-    }
-    if (P.dealias == 1) {
-      if (kx >= K.kxlim[kz * g.ny + ky]) un = cx_zero<T>();
-    } else if (P.dealias == 2) {
-      un = ((un * K.fx[kx]) * K.fy[ky]) * K.fz[kz];
-    }
-    Store<T>::stc(U + idx, un);
   }
 }
 

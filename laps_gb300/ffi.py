@@ -43,6 +43,8 @@ class laps_params(C.Structure):
         ("if_AEB", C.c_int), ("radius0", C.c_double), ("Ur0", C.c_double),
         ("if_corotating", C.c_int), ("corotating_angle", C.c_double),
         ("if_Hall", C.c_int), ("ion_inertial_length", C.c_double),
+        ("rho0", C.c_double), ("if_z_radial", C.c_int), ("if_limit_dt_increase", C.c_int),
+        ("dstep_calcdt", C.c_int),
         ("device", C.c_int), ("timeout_ms", C.c_int), ("mem_cap_bytes", C.c_longlong),
         ("reserved", C.c_int * 8),
     ]
@@ -52,7 +54,8 @@ class laps_diag(C.Structure):
     _fields_ = [
         ("time", C.c_double), ("dt", C.c_double), ("radius", C.c_double),
         ("uu_ave", C.c_double * 8), ("uu_rms", C.c_double * 8), ("rho_u2", C.c_double * 3),
-        ("max_divB", C.c_double), ("e_kin", C.c_double), ("e_mag", C.c_double),
+        ("max_divB", C.c_double), ("max_divB_real", C.c_double), ("max_divV_real", C.c_double),
+        ("e_kin", C.c_double), ("e_mag", C.c_double),
         ("h_cross", C.c_double), ("h_mag", C.c_double),
     ]
 

@@ -332,10 +332,7 @@ class Laps3DC:
         f[17] = (uu[EN] + ptot) * uz - udotb * Bz
         expand = None
         if p.if_AEB:
-            tau = self.tau_exp
-            expand = (-2 * g / (g - 1) * P / tau
-                      - (2.0 * Bx**2 + By**2 + Bz**2) / tau
-                      - (uu[MX] * ux + 2 * uu[MY] * uy + 2 * uu[MZ] * uz) / tau)
+            expand = self.expand_term(P, Bx, By, Bz, uu, ux, uy, uz, g, self.tau_exp)
         if p.if_Hall:
             J = self.calc_current_density_real()
             di = p.ion_inertial_length
@@ -343,6 +340,16 @@ class Laps3DC:
             f[13] = f[13] + di / rho * (J[2] * uu[BX] - J[0] * uu[BZ])
             f[14] = f[14] + di / rho * (J[0] * uu[BY] - J[1] * uu[BX])
         return f, expand
+
+    def expand_term(self, P, Bx, By, Bz, uu, ux, uy, uz, g, tau):
+        """Energy source of the expanding box (``mhdrhs.f90:93-103``)."""
+        return (-2 * g / (g - 1) * P / tau
+                - (2.0 * Bx**2 + By**2 + Bz**2) / tau
+                - (uu[MX] * ux + 2 * uu[MY] * uy + 2 * uu[MZ] * uz) / tau)
+
+    def expansion_coefficients(self):
+        """Damping factors of rho, rho u, B in calc_rhs (``mhdrhs.f90:235-247``)."""
+        return (2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0)
 
     def transform_flux_real_to_fourier(self, flux, expand):
         """``mhdrhs.f90:128-172``."""
@@ -367,7 +374,7 @@ class Laps3DC:
         fnl[7] = -(i * kx * ff[15] + i * ky * ff[16] + i * kz * ff[17])
         if p.if_AEB:
             tau = self.tau_exp
-            for v, c in ((0, 2.0), (1, 2.0), (2, 3.0), (3, 3.0), (4, 2.0), (5, 1.0), (6, 1.0)):
+            for v, c in enumerate(self.expansion_coefficients()):
                 fnl[v] = fnl[v] - c * uf[v] / tau
             fnl[7] = fnl[7] + ef
         if p.if_visc and p.if_visc_exp:
@@ -457,11 +464,13 @@ class Laps3DC:
         return self.dt
 
     def step(self):
-        """evolve; time += dt; evolve_radius(time); vardt (``mhd.f90:245-285``)."""
+        """One step as laps_step takes it: vardt; evolve; time += dt; evolve_radius(time) -
+        the loop body of ``mhd.f90:245-285`` with its trailing vardt moved to the front (the
+        first call plays the vardt before the loop, ``mhd.f90:135-136``)."""
+        self.vardt()
         self.evolve()
         self.time = self.time + self.dt
         self.evolve_radius(self.time)
-        self.vardt()
 
     def calc_max_divB(self):
         """max |ik . B_hat| over the spectral grid (``mhd.f90:522-570``)."""
@@ -532,6 +541,331 @@ def restart(n, kw, prim, t0=0.0) -> Laps3DC:
     """Start as the reference's restart path does: read primitives, evolve_radius(t0),
     conserve, forward transform (src_compressible/mhd.f90:101-122)."""
     o = Laps3DC(params_from(n, kw))
+    o.initial_calc_conserve_variable(prim)
+    o.time = t0
+    o.evolve_radius(t0)
+    o.transform_uu_real_to_fourier()
+    return o
+
+
+# ============================================================================ 2-D compressible
+@dataclasses.dataclass
+class Params2D(Params3D):
+    """Namelist values of the 2-D compressible code (``src_compressible/2D/mhd.f90:33-43``);
+    nz = 1.  ``if_limit_dt_increase`` and the vardt cadence ``dstep_calcdt``
+    (``src_compressible/2D/mhd.f90:20,23``) are 2-D only."""
+
+    nz: int = 1
+    if_z_radial: bool = False
+    if_limit_dt_increase: bool = False
+    dstep_calcdt: int = 20
+
+
+class Laps2DC(Laps3DC):
+    """2-D compressible solver: the 3-D routines with kz = 0 and the 2-D differences
+    (``src_compressible/2D/``): radial-z expansion geometry, square dealias option 3, the
+    explicit-eta CFL term and vardt every ``dstep_calcdt`` steps."""
+
+    def __init__(self, p: Params2D):
+        assert p.nz == 1
+        super().__init__(p)
+        self.wz = np.zeros(1)
+        self.zrad = bool(p.if_AEB and p.if_z_radial)
+        self.k_square = self.wx[None, None, :] ** 2 + self.wy[None, :, None] ** 2
+        self.dz = None
+        self.istep = 0
+
+    def _init_dealias(self):
+        p = self.p
+        if p.dealias_option == 1:
+            rx = (self.wx * p.Lx / (2 * PI * p.nx)) ** 2
+            ry = (self.wy * p.Ly / (2 * PI * p.ny)) ** 2
+            rad = np.sqrt(rx[None, None, :] + ry[None, :, None])
+            self.keep = ~(rad > 1.0 / 3.0)
+        elif p.dealias_option == 3:  # square 2/3 truncation, 2D/dealiasing.f90:102-117
+            rx = np.abs(self.wx * p.Lx / (2 * PI * p.nx))
+            ry = np.abs(self.wy * p.Ly / (2 * PI * p.ny))
+            self.keep = ~((rx[None, None, :] > 1.0 / 3.0) | (ry[None, :, None] > 1.0 / 3.0))
+        elif p.dealias_option == 2:
+            super()._init_dealias()
+            self.filtz = np.ones(1)
+
+    def dealias(self):
+        p = self.p
+        if p.dealias_option in (1, 3):
+            self.uf[:, ~self.keep] = 0.0
+        elif p.dealias_option == 2:
+            self.uf = (self.uf * self.filtx[None, None, None, :]) * self.filty[None, None, :, None]
+
+    def evolve_radius(self, t):
+        """``src_compressible/2D/AEBmod.f90``: k^2 without kz; radial-z scales kx too."""
+        p = self.p
+        self.radius = p.radius0 + self.Ur0 * t
+        self.tau_exp = self._tau(self.radius)
+        kx = self.wx[None, None, :]
+        ky = self.wy[None, :, None]
+        R0, R = p.radius0, self.radius
+        if p.if_corotating:
+            c, s = self.cos_cor, self.sin_cor
+            self.k_square = (kx**2 * (c**2 + (s * R0 / R) ** 2) + ky**2 * (s**2 + (c * R0 / R) ** 2)
+                             + kx * ky * 2 * c * s * (1 - (R0 / R) ** 2))
+        elif p.if_z_radial:
+            self.k_square = (kx * R0 / R) ** 2 + (ky * R0 / R) ** 2
+        else:
+            self.k_square = kx**2 + (ky * R0 / R) ** 2
+
+    def ik(self):
+        """``src_compressible/2D/mhdrhs.f90:272-288``: kz = 0; radial-z scales kx by R0/R."""
+        kx, ky, kz = super().ik()
+        if self.zrad and not (self.p.if_AEB and self.p.if_corotating):
+            kx = kx * self.p.radius0 / self.radius
+        return kx, ky, np.zeros_like(kz)
+
+    def expansion_coefficients(self):
+        """(rho, rho u, B) damping factors of calc_rhs (``2D/mhdrhs.f90:319-343``)."""
+        if self.zrad:
+            return (2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 2.0)
+        return (2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0)
+
+    def expand_term(self, P, Bx, By, Bz, uu, ux, uy, uz, g, tau):
+        if self.zrad:  # 2D/mhdrhs.f90:96-100
+            return (-2 * g / (g - 1) * P / tau - (Bx**2 + By**2 + 2.0 * Bz**2) / tau
+                    - (2 * uu[MX] * ux + 2 * uu[MY] * uy + uu[MZ] * uz) / tau)
+        return super().expand_term(P, Bx, By, Bz, uu, ux, uy, uz, g, tau)
+
+    def vardt_min(self):
+        """``src_compressible/2D/mhd.f90:294-394``: x and y only, explicit-eta term, radial x."""
+        p = self.p
+        uu, pr = self.uu, self.uu_prim
+        rho = uu[RHO]
+        cs2 = p.adiabatic_index * pr[3] / rho
+        sq = np.sqrt(rho)
+        cax, cay, caz = uu[BX] / sq, uu[BY] / sq, uu[BZ] / sq
+        ca2 = cax**2 + cay**2 + caz**2
+        cms2 = cs2 + ca2
+        s2 = math.sqrt(2.0)
+        cmax = []
+        for ca, u in ((cax, pr[0]), (cay, pr[1])):
+            cns2 = np.sqrt(np.maximum(cms2**2 - 4 * cs2 * ca**2, 0.0))
+            cf = np.sqrt(cms2 + cns2) / s2
+            csl = np.sqrt(np.maximum(cms2 - cns2, 0.0)) / s2
+            cmax.append(np.maximum.reduce([np.abs(u + cf), np.abs(u + csl), np.abs(u + ca),
+                                           np.abs(u - cf), np.abs(u - csl), np.abs(u - ca), np.abs(u)]))
+        if p.if_resis and p.if_resis_exp:
+            cmax = [np.maximum(cmax[0], p.resistivity / self.dx), np.maximum(cmax[1], p.resistivity / self.dy)]
+        if p.if_Hall:
+            ch = p.ion_inertial_length / rho * np.maximum(np.maximum(uu[BX], uu[BY]), uu[BZ]) / min(self.dx, self.dy)
+            cmax = [np.maximum(c, ch) for c in cmax]
+        with np.errstate(divide="ignore"):
+            dtx = self.dx / cmax[0]
+            if p.if_AEB and p.if_z_radial:
+                dtx = dtx * (self.radius / p.radius0)
+            dty = self.dy / cmax[1] * (self.radius / p.radius0)
+        return float(np.min(np.minimum(dtx, dty)))
+
+    def vardt(self):
+        """dt = cfl * min; +-2 % hysteresis, or with if_limit_dt_increase only a decrease (or
+        the first call) replaces dt (``2D/mhd.f90:396-405``)."""
+        dtmin = self.vardt_min() * self.p.cfl
+        if self.p.if_limit_dt_increase:
+            if self.dt == 0.0 or self.dt > 1.02 * dtmin:
+                self.dt = dtmin
+        elif self.dt < 0.98 * dtmin or self.dt > 1.02 * dtmin:
+            self.dt = dtmin
+        self.rkt_init(self.dt)
+        return self.dt
+
+    def step(self):
+        """Loop body of ``2D/mhd.f90:196-240``, with vardt at the front of the step when
+        istep is a multiple of dstep_calcdt (istep = 0 is the call before the loop)."""
+        if self.istep % self.p.dstep_calcdt == 0:
+            self.vardt()
+        self.evolve()
+        self.time = self.time + self.dt
+        self.istep += 1
+        self.evolve_radius(self.time)
+
+
+def restart2d(n, kw, prim, t0=0.0) -> Laps2DC:
+    nx, ny = (n, n) if np.isscalar(n) else n[:2]
+    p = Params2D(nx=nx, ny=ny, nz=1)
+    for k, v in kw.items():
+        if hasattr(p, k):
+            cur = getattr(p, k)
+            setattr(p, k, bool(v) if isinstance(cur, bool) else type(cur)(v))
+    o = Laps2DC(p)
+    o.initial_calc_conserve_variable(prim)
+    o.time = t0
+    o.evolve_radius(t0)
+    o.transform_uu_real_to_fourier()
+    return o
+
+
+# ============================================================================ 3-D incompressible
+@dataclasses.dataclass
+class Params3DI(Params3D):
+    """``src_incompressible``: rho0 is the module default of mhdinit.f90:15 (not a namelist
+    value); it divides the velocity gradient and decays with the expanding box."""
+
+    rho0: float = 1.0
+
+
+class Laps3DI(Laps3DC):
+    """3-D incompressible solver (``src_incompressible/``).  State slots: 1 rho, 2:4 rho u,
+    5:7 B, 8 pressure p (no energy); uu_prim = u."""
+
+    def initial_calc_conserve_variable(self, prim):
+        """rho u = rho * u; p kept (``src_incompressible/mhdinit.f90:1031-1042``)."""
+        uu = np.array(prim, dtype=np.float64, copy=True)
+        self.uu_prim = uu[1:4].copy()
+        uu[1] = uu[0] * self.uu_prim[0]
+        uu[2] = uu[0] * self.uu_prim[1]
+        uu[3] = uu[0] * self.uu_prim[2]
+        self.uu = uu
+        self.rho0 = self.p.rho0
+
+    def update_uu_prim_from_uu(self):
+        """``src_incompressible/mhdrhs.f90:235-242``."""
+        uu = self.uu
+        self.uu_prim = np.stack([uu[1] / uu[0], uu[2] / uu[0], uu[3] / uu[0]])
+
+    def calc_gradient_velocity_real(self):
+        """grad(rho u)/rho0, 9 inverse transforms (``src_incompressible/mhdrhs.f90:312-391``):
+        order d(ux)/dx, d(ux)/dy, d(ux)/dz, d(uy)/dx, ..."""
+        kx, ky, kz = self.ik()
+        uf = self.uf
+        gf = []
+        for v in (MX, MY, MZ):
+            for k in (kx, ky, kz):
+                gf.append(1j * k * uf[v])
+        gf = np.stack(gf) / self.rho0
+        return inverse_3d(gf, self.p.nx)
+
+    def stage(self, irk):
+        """One RK stage of the incompressible evolve (``src_incompressible/mhd.f90:323-363``)."""
+        p = self.p
+        self.transform_uu_real_to_fourier()
+        J = self.calc_current_density_real()
+        G = self.calc_gradient_velocity_real()
+        uu = self.uu
+        # calc_flux_for_pressure, src_incompressible/mhdrhs.f90:393-437
+        fp = np.stack([
+            -uu[MX] * G[0] - uu[MY] * G[1] - uu[MZ] * G[2] + J[1] * uu[BZ] - J[2] * uu[BY],
+            -uu[MX] * G[3] - uu[MY] * G[4] - uu[MZ] * G[5] + J[2] * uu[BX] - J[0] * uu[BZ],
+            -uu[MX] * G[6] - uu[MY] * G[7] - uu[MZ] * G[8] + J[0] * uu[BY] - J[1] * uu[BX],
+        ])
+        fpf = forward_3d(fp)
+        kx, ky, kz = self.ik()
+        k2 = self.k_square
+        small = k2 < 1e-10
+        with np.errstate(divide="ignore", invalid="ignore"):
+            kdot = (1j * kx * fpf[0] + 1j * ky * fpf[1] + 1j * kz * fpf[2]) / np.where(small, 1.0, k2)
+        kdot = np.where(small, 0.0, kdot)
+        # calc_pressure_fourier, :468-518
+        self.uf[EN] = np.where(small, 0.0, -kdot)
+        # calc_flux (electric field), :25-84
+        pr = self.uu_prim
+        E = np.stack([pr[2] * uu[BY] - pr[1] * uu[BZ], pr[0] * uu[BZ] - pr[2] * uu[BX], pr[1] * uu[BX] - pr[0] * uu[BY]])
+        if p.if_Hall:
+            di = p.ion_inertial_length
+            E[0] = E[0] + di / uu[RHO] * (J[1] * uu[BZ] - J[2] * uu[BY])
+            E[1] = E[1] + di / uu[RHO] * (J[2] * uu[BX] - J[0] * uu[BZ])
+            E[2] = E[2] + di / uu[RHO] * (J[0] * uu[BY] - J[1] * uu[BX])
+        Ef = forward_3d(E)
+        # calc_rhs, :117-232
+        uf = self.uf
+        fnl = np.zeros_like(uf)
+        fnl[1] = np.where(small, 0.0, fpf[0] + kdot * 1j * kx)
+        fnl[2] = np.where(small, 0.0, fpf[1] + kdot * 1j * ky)
+        fnl[3] = np.where(small, 0.0, fpf[2] + kdot * 1j * kz)
+        fnl[4] = 1j * kz * Ef[1] - 1j * ky * Ef[2]
+        fnl[5] = 1j * kx * Ef[2] - 1j * kz * Ef[0]
+        fnl[6] = 1j * ky * Ef[0] - 1j * kx * Ef[1]
+        if p.if_AEB:
+            tau = self.tau_exp
+            for v, c in ((0, 2.0), (1, 2.0), (2, 3.0), (3, 3.0), (4, 2.0), (5, 1.0), (6, 1.0)):
+                fnl[v] = fnl[v] - c * uf[v] / tau
+            fnl[7] = fnl[7] - 2.0 * p.adiabatic_index * uf[7] / tau
+        if p.if_visc and p.if_visc_exp:
+            for v in (1, 2, 3):
+                fnl[v] = fnl[v] - p.viscosity * uf[v] * k2
+        if p.if_resis and p.if_resis_exp:
+            m = np.ones(k2.shape, bool)
+            if p.if_conserve_background:
+                m[0, :, 0] = False
+            for v in (4, 5, 6):
+                fnl[v] = np.where(m, fnl[v] - p.resistivity * uf[v] * k2, fnl[v])
+        self.rkt(irk, fnl)
+        self.dealias()
+        self.transform_uu_fourier_to_real()
+        self.update_uu_prim_from_uu()
+
+    def evolve(self):
+        for irk in (1, 2, 3):
+            self.stage(irk)
+        # update_rho_p (src_incompressible/AEBmod.f90:123-134), at the step's start radius
+        self.rho0 = self.rho0 * (self.p.radius0 / self.radius) ** 2
+
+    def vardt_min(self):
+        """Alfven-only CFL (``src_incompressible/mhd.f90:394-463``)."""
+        p = self.p
+        uu, pr = self.uu, self.uu_prim
+        rho = uu[RHO]
+        sq = np.sqrt(rho)
+        cmax = []
+        for b, u in ((BX, pr[0]), (BY, pr[1]), (BZ, pr[2])):
+            ca = uu[b] / sq
+            cmax.append(np.maximum.reduce([np.abs(u + ca), np.abs(u - ca), np.abs(u)]))
+        if p.if_Hall:
+            ch = p.ion_inertial_length / rho * np.maximum(np.maximum(uu[BX], uu[BY]), uu[BZ]) / min(
+                self.dx, self.dy, self.dz)
+            cmax = [np.maximum(c, ch) for c in cmax]
+        with np.errstate(divide="ignore"):
+            dtx = self.dx / cmax[0]
+            dty = self.dy / cmax[1] * (self.radius / p.radius0)
+            dtz = self.dz / cmax[2] * (self.radius / p.radius0)
+        return float(np.min(np.minimum(np.minimum(dtx, dty), dtz)))
+
+    def calc_rms(self):
+        """``src_incompressible/mhdrms.f90:47-120``.  Its p columns read uu_prim(:,:,:,4),
+        beyond the 3 components uu_prim has here, and are undefined; the pressure held in
+        slot 8 is reported there instead."""
+        uu, pr = self.uu, self.uu_prim
+        n = uu[0].size
+        f = [uu[RHO], pr[0], pr[1], pr[2], uu[BX], uu[BY], uu[BZ], uu[EN]]
+        ave = np.array([np.sum(a) for a in f]) / n
+        sq = np.array([np.sum(a * a) for a in f]) / n
+        rms = sq - ave**2
+        rho_u2 = np.array([np.sum(uu[RHO] * (pr[i] - ave[1 + i]) ** 2) for i in range(3)]) / n
+        return ave, rms, rho_u2
+
+    def div_maxima(self):
+        """max |div B| and max |div(rho u)|/rho0 in real space (calc_divB_real,
+        calc_divV_real and their maxima: src_incompressible/mhdrhs.f90:532-648,
+        mhd.f90:672-732)."""
+        kx, ky, kz = self.ik()
+        uf = self.uf
+        db = inverse_3d(1j * kx * uf[BX] + 1j * ky * uf[BY] + 1j * kz * uf[BZ], self.p.nx)
+        dv = inverse_3d((1j * kx * uf[MX] + 1j * ky * uf[MY] + 1j * kz * uf[MZ]) / self.rho0, self.p.nx)
+        return float(np.max(np.abs(db))), float(np.max(np.abs(dv)))
+
+    def invariants(self):
+        uu, pr = self.uu, self.uu_prim
+        ekin = 0.5 * np.mean(uu[RHO] * (pr[0] ** 2 + pr[1] ** 2 + pr[2] ** 2))
+        emag = 0.5 * np.mean(uu[BX] ** 2 + uu[BY] ** 2 + uu[BZ] ** 2)
+        hc = np.mean(pr[0] * uu[BX] + pr[1] * uu[BY] + pr[2] * uu[BZ])
+        hm = magnetic_helicity(self.uf[BX:BZ + 1], *self.ik(), self.p.nx)
+        return np.array([ekin, emag, hc, hm])
+
+
+def restart3di(n, kw, prim, t0=0.0) -> Laps3DI:
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    p = Params3DI(nx=nx, ny=ny, nz=nz)
+    for k, v in kw.items():
+        if hasattr(p, k):
+            cur = getattr(p, k)
+            setattr(p, k, bool(v) if isinstance(cur, bool) else type(cur)(v))
+    o = Laps3DI(p)
     o.initial_calc_conserve_variable(prim)
     o.time = t0
     o.evolve_radius(t0)

@@ -60,7 +60,12 @@ def test_defaults_are_reference_initialisers(lib):
         (dict(nx=100), ffi.LAPS_EINVAL),
         (dict(nx=64, ny=48, nz=64), ffi.LAPS_EINVAL),
         (dict(nx=64, ny=64, nz=64, precision=7), ffi.LAPS_EINVAL),
-        (dict(nx=64, ny=64, nz=64, variant=1), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, variant=5), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=8, variant=2), ffi.LAPS_EINVAL),  # 2-D needs nz = 1
+        (dict(nx=64, ny=64, nz=1, variant=0), ffi.LAPS_EINVAL),  # 3-D needs nz >= 8
+        (dict(nx=64, ny=64, nz=1, variant=2, if_AEB=1, if_z_radial=1, if_corotating=1), ffi.LAPS_EINVAL),
+        (dict(nx=1024, ny=64, nz=64), ffi.LAPS_EINVAL),
+        (dict(nx=64, ny=64, nz=64, variant=1, rho0=0.0), ffi.LAPS_EINVAL),
         (dict(nx=64, ny=64, nz=64, cfl=0.0), ffi.LAPS_EINVAL),
         (dict(nx=64, ny=64, nz=64, mem_cap_bytes=1 << 20), ffi.LAPS_ENOMEM),
     ],

@@ -17,7 +17,7 @@ def test_golden_case(path, prec):
     g = np.load(path)
     nx, ny, nz = (int(v) for v in g["shape"])
     kw = eval(str(g["params"]))  # a dict literal written by make_golden.py
-    run = ffi.Laps(ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, **kw))
+    run = ffi.Laps(ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, **kw))  # kw may carry "variant"
     run.upload_state(g["prim"], primitive=True)
     run.set_time(0.0)
     t, dt, status = run.step(int(g["steps"]))
