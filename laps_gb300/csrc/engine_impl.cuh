@@ -309,6 +309,7 @@ template <class T> class Engine : public EngineBase {
   PassArgs args(const Geo& g, int stage, int store_rk, int cfl) {
     PassArgs a;
     a.g = g; a.P = P; a.hall = P.hall; a.aeb = P.aeb; a.stage = stage; a.store_rk = store_rk; a.cfl = cfl; a.st = st;
+    a.mass_from_state = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
     return a;
   }
   void passA(const PassArgs& a) { launch_passA<T>(stream, p.nz, B, a, pc, ktab(), twz); }

@@ -16,6 +16,9 @@ struct PassArgs {
   int stage;       // 0, 1, 2
   int store_rk;    // write fnl_rk (not needed after the last stage of a fused step)
   int cfl;         // pass C: 0 fluxes, 1 fluxes + CFL minimum, 2 CFL minimum only
+  int mass_from_state;  // compressible, Nyquist modes zeroed by the dealiasing: the mass
+                        // flux rho u is the state's momentum, so -i k.(rho u)^ is taken from U
+                        // in pass E and passes C, D skip fluxes 1..3
   StepState* st;
 };
 
@@ -342,7 +345,8 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   SR* sr = reinterpret_cast<SR*>(smem_raw);
   const Geo& g = a.g;
   const int nin = INCOMP ? 19 : (a.hall ? 11 : 8);
-  const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.aeb ? 19 : 18));  // a.cfl == 2: CFL minimum only
+  const int f0 = (!INCOMP && a.mass_from_state) ? 3 : 0;  // first flux transformed
+  const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.aeb ? 19 : 18)) - f0;  // a.cfl == 2: CFL minimum only
   long long row0 = (long long)blockIdx.x * CF::ROWS;  // row = z*ny + y
   const int lt = threadIdx.x % CF::TPL, lb = threadIdx.x / CF::TPL;
   // ---- c2r of the inputs
@@ -379,7 +383,7 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
       if (Real<T>::isnan_(d)) nan_seen = true;
       else tmin = Real<T>::min_(tmin, d);
     }
-    if (nfl > 0) PH::eval(q, [&](int k, T v) { Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
+    if (nfl > 0) PH::eval(q, [&](int k, T v) { if (k >= f0) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   if (CFL) {
     double dmin = Real<T>::to_d(tmin);
@@ -399,7 +403,7 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   for (int L0 = 0; L0 < CF::ROWS * nfl; L0 += CF::LB) {
     int L = L0 + lb;
     bool act = L < CF::ROWS * nfl;
-    int rr = act ? L / nfl : 0, f = act ? L % nfl : 0;
+    int rr = act ? L / nfl : 0, f = act ? f0 + L % nfl : 0;
     C* z = sc + (rr * CF::NF + f) * CF::LC;
     fft_lines<T, CF::H, -1, 1, 0>(z, 0, lt, act, twx, 2);
     if (act) {
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
   if (a.st->halt) return;
   ColCtx<T, NY, 2> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
-  const DGroup grp = c_dgroups[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][blockIdx.z];
+  const DGroup grp = c_dgroups[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][blockIdx.z + (a.mass_from_state ? 2 : 0)];
   int kx = blockIdx.x * TX + x.c;
   int z = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && z < g.nz;
@@ -586,7 +590,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
   // in 2-D, where kz = 0)
   const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
   const int in2 = (v == 6 || a.P.two_d) ? -1 : v == 4 ? 9 : v == 5 ? 8 : v == 7 ? 14 : 2 * v + 1;
-  const int nin = in2 < 0 ? 1 : 2;
+  const int nin = (v == 0 && a.mass_from_state) ? 0 : (in2 < 0 ? 1 : 2);
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
     const C* in = b.W2 + (k == 0 ? in1 : in2) * g.fsc + col;
@@ -607,8 +611,17 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     if (!g.kz_in(kz)) continue;
-    cx<T> fnl = Store<T>::ldc(x.at(0, m));
-    fnl = {Real<T>::mul_pow2(fnl.re, sexp), Real<T>::mul_pow2(fnl.im, sexp)};
+    cx<T> fnl;
+    if (nin == 0) {  // continuity: -i k . (rho u)^ from the momentum spectrum (mhdrhs.f90:206-209)
+      T ax, ay, az;
+      kfac(K, a.P, pc, rk.rr, kx, ky, kz, ax, ay, az);
+      const long long id = kz * zs;
+      fnl = -((mul_i(Store<T>::ldg(b.U + 1 * g.fsc + col + id), ax) + mul_i(Store<T>::ldg(b.U + 2 * g.fsc + col + id), ay)) +
+              mul_i(Store<T>::ldg(b.U + 3 * g.fsc + col + id), az));
+    } else {
+      fnl = Store<T>::ldc(x.at(0, m));
+      fnl = {Real<T>::mul_pow2(fnl.re, sexp), Real<T>::mul_pow2(fnl.im, sexp)};
+    }
     if (nin > 1) {
       cx<T> w = Store<T>::ldc(x.at(1, m));
       w = mul_i(cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)}, K.kzd[kz]);
