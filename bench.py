@@ -39,6 +39,7 @@ N_GRID = 256
 WORKLOAD = "3D compressible Hall-MHD + expanding box, 256^3"
 CFG2 = dict(if_resis=1, resistivity=5e-4, if_visc=1, viscosity=5e-4, dealias_option=1, cfl=0.4,
             if_Hall=1, ion_inertial_length=0.05, if_AEB=1, radius0=30.0, Ur0=0.3)
+SHAPE = None  # (nx, ny, nz) of a reduced profiling case
 PASS_NAMES = ["A_inv_z", "B_inv_y", "C_x_flux", "D_fwd_y", "E_fwd_z_rk", "bookkeeping"]
 
 
@@ -70,7 +71,7 @@ def barrier(ws):
 def initial_state(n=None):
     from laps_gb300.ic import turbulence_ic
 
-    n = n or N_GRID
+    n = n or (SHAPE if SHAPE else N_GRID)
     return turbulence_ic(n, kmin=1, kmax=8, alpha=-1.0, rms_u=0.5, rms_b=0.5, seed=1)
 
 
@@ -192,8 +193,10 @@ def run_ours(args):
 
     prec = {"dd": ffi.PREC_DD, "fp64": ffi.PREC_FP64}[args.precision]
     n = N_GRID
-    prim = initial_state(n)
-    p = ffi.params(nx=n, ny=n, nz=n, precision=prec, device=local, **CFG2)
+    prim = initial_state()
+    nx, ny, nz = SHAPE if SHAPE else (n, n, n)
+    npts = nx * ny * nz
+    p = ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, device=local, **CFG2)
     g = ffi.Laps(p)
     g.upload_state(prim, primitive=True)
     g.set_time(0.0)
@@ -205,7 +208,7 @@ def run_ours(args):
         pass_ms, total_ms, status = g.step_profiled(args.steps)
     barrier(ws)
     tmax = barrier_max(total_ms, ws)
-    value = ws * n**3 * args.steps / (tmax * 1e-3)
+    value = ws * npts * args.steps / (tmax * 1e-3)
     # ---- graph path, same state continues (reported beside)
     t0 = time.perf_counter()
     g.step(args.steps)
@@ -240,18 +243,18 @@ def run_ours(args):
                                  host_prim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert rc == 0
     e2e_s = barrier_max(time.perf_counter() - t0, ws)
-    e2e_v = ws * n**3 * args.steps / e2e_s
+    e2e_v = ws * npts * args.steps / e2e_s
     h2d = host_in.nbytes / args.steps + 16
     d2h = (host_out.nbytes + host_prim.nbytes) / args.steps + 128
     e2e_ctx.close()
     # ---- roofline of the dominant pass
     nky, nkz = info.ky_keep, info.kz_keep
-    pb = pass_bytes(n, info.kx_keep, nky, nkz)
+    pb = pass_bytes(n, info.kx_keep, nky, nkz) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
     launches = args.steps * 3
     dom = max(range(5), key=lambda i: pass_ms[i])
     name = PASS_NAMES[dom]
     avg_ms = pass_ms[dom] / launches
-    achieved = pb[name] / (avg_ms * 1e-3) / 1e9
+    achieved = pb[name] / (avg_ms * 1e-3) / 1e9 if pb[name] else None
     peak, src = peaks()
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
@@ -273,7 +276,7 @@ def run_ours(args):
         "graph_ms_per_step": graph_ms,
         "pass_ms_per_step": {PASS_NAMES[i]: pass_ms[i] / args.steps for i in range(6)},
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+                     "frac": achieved / peak if achieved else None, "peak_source": src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": pb[name]},
         "e2e": {"value": e2e_v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "pinned": pinned},
@@ -303,7 +306,12 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
     ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")
     ap.add_argument("--grid", type=int, default=256, help="grid size n (n^3); the headline workload is 256")
+    ap.add_argument("--shape", default=None, help="nx,ny,nz of a reduced profiling case (overrides --grid)")
     args = ap.parse_args()
+    global SHAPE
+    if args.shape:
+        SHAPE = tuple(int(v) for v in args.shape.split(","))
+        WORKLOAD = f"3D compressible Hall-MHD + expanding box, {args.shape} (reduced case)"
     if args.grid != N_GRID:
         N_GRID = args.grid
         WORKLOAD = f"3D compressible Hall-MHD + expanding box, {N_GRID}^3 (reduced case)"

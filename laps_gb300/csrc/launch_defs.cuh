@@ -87,7 +87,7 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passD<T, NN>, 2 * CL::SMEM);                                                                             \
-    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : (a.mass_from_state ? 10 : 12)); \
+    dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : (a.mass_from_state ? 6 : 8)); \
     k_passD<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
     break;                                                                                                              \
   }

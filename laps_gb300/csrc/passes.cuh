@@ -321,6 +321,14 @@ struct FluxI {
 
 // rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
 // (Hall) in one batch and their 38 outputs in two
+// pass C transform lists (flux slot numbers): compressible, compressible with the continuity
+// term from the state, incompressible; the expansion term 18 is last and dropped without it
+__constant__ int c_flist[3][16] = {{0, 1, 2, 3, 4, 5, 7, 8, 11, 12, 13, 14, 15, 16, 17, 18},
+                                   {3, 4, 5, 7, 8, 11, 12, 13, 14, 15, 16, 17, 18, 0, 0, 0},
+                                   {0, 1, 2, 3, 4, 5, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
+// slots the physics has to store (all but 6, 9, 10; in the incompressible case all of 0..5)
+constexpr unsigned c_fused = 0x7FFFFu & ~((1u << 6) | (1u << 9) | (1u << 10));
+
 template <int NX> struct PassCCfg {
   static constexpr int H = NX / 2;
   static constexpr int TPL = Plan<H>::TPL;
@@ -345,8 +353,11 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   SR* sr = reinterpret_cast<SR*>(smem_raw);
   const Geo& g = a.g;
   const int nin = INCOMP ? 19 : (a.hall ? 11 : 8);
-  const int f0 = (!INCOMP && a.mass_from_state) ? 3 : 0;  // first flux transformed
-  const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.aeb ? 19 : 18)) - f0;  // a.cfl == 2: CFL minimum only
+  // fluxes transformed, in order: the momentum flux tensor is symmetric (T_xy = T_yx,
+  // T_xz = T_zx, T_yz = T_zy), so slots 6, 9, 10 are never needed; slots 0..2 are skipped
+  // when the continuity term comes from the state
+  const int* flist = INCOMP ? c_flist[2] : c_flist[a.mass_from_state ? 1 : 0];
+  const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.mass_from_state ? 13 : 16) - (a.aeb ? 0 : 1));
   long long row0 = (long long)blockIdx.x * CF::ROWS;  // row = z*ny + y
   const int lt = threadIdx.x % CF::TPL, lb = threadIdx.x / CF::TPL;
   // ---- c2r of the inputs
@@ -383,7 +394,7 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
       if (Real<T>::isnan_(d)) nan_seen = true;
       else tmin = Real<T>::min_(tmin, d);
     }
-    if (nfl > 0) PH::eval(q, [&](int k, T v) { if (k >= f0) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
+    if (nfl > 0) PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   if (CFL) {
     double dmin = Real<T>::to_d(tmin);
@@ -403,7 +414,7 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
   for (int L0 = 0; L0 < CF::ROWS * nfl; L0 += CF::LB) {
     int L = L0 + lb;
     bool act = L < CF::ROWS * nfl;
-    int rr = act ? L / nfl : 0, f = act ? f0 + L % nfl : 0;
+    int rr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
     C* z = sc + (rr * CF::NF + f) * CF::LC;
     fft_lines<T, CF::H, -1, 1, 0>(z, 0, lt, act, twx, 2);
     if (act) {
@@ -428,10 +439,16 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
 // One group per blockIdx.z; tile: kx0..kx0+7, one z plane; reads all y of W1, writes kept
 // ky rows of W2.
 struct DGroup { signed char in[3], kind, out; };
-enum { DG_Q = 0, DG_COPY, DG_EXY, DG_EZ, DG_Q8 };
-__constant__ DGroup c_dgroups[2][12] = {
-    {{{0, 1, -1}, DG_Q, 0},  {{2, -1, -1}, DG_COPY, 1},  {{3, 4, -1}, DG_Q, 2},    {{5, -1, -1}, DG_COPY, 3},
-     {{6, 7, -1}, DG_Q, 4},  {{8, -1, -1}, DG_COPY, 5},  {{9, 10, -1}, DG_Q, 6},   {{11, -1, -1}, DG_COPY, 7},
+// kinds: Q:    out = -(i ax F_a + i ay F_b)
+//        COPY: out = F_a
+//        EXY:  out, out+1, out+2 = Ex, Ey, i ay Ex - i ax Ey
+//        EZ:   out, out+1 = -i ay Ez, i ax Ez
+//        Q8:   out = -(i ax F_a + i ay F_b) (+ expansion term F_c)
+//        QQ:   (F3, F4 = F6, F7) -> out = Q2 = -(i ax Txx + i ay Tyx), out+2 = Q3 = -(i ax Txy + i ay Tyy)
+//        T3:   (F5 = F9, F8 = F10, F11) -> out = Tzx, out+2 = Tzy, out+3 = Q4 = -(i ax Txz + i ay Tyz), out+4 = Tzz
+enum { DG_Q = 0, DG_COPY, DG_EXY, DG_EZ, DG_Q8, DG_QQ, DG_T3 };
+__constant__ DGroup c_dgroups[2][8] = {
+    {{{0, 1, -1}, DG_Q, 0}, {{2, -1, -1}, DG_COPY, 1}, {{3, 4, 7}, DG_QQ, 2}, {{5, 8, 11}, DG_T3, 3},
      {{12, 13, -1}, DG_EXY, 8}, {{14, -1, -1}, DG_EZ, 11}, {{15, 16, 18}, DG_Q8, 13}, {{17, -1, -1}, DG_COPY, 14}},
     {{{0, -1, -1}, DG_COPY, 0}, {{1, -1, -1}, DG_COPY, 1}, {{2, -1, -1}, DG_COPY, 2}, {{3, 4, -1}, DG_EXY, 3},
      {{5, -1, -1}, DG_EZ, 6}}};
@@ -451,10 +468,12 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
   long long col = (long long)z * g.ny * g.kxp + kx;
   T rr = Real<T>::from_d(a.st->r_ratio);
   const int sexp = -__ffs(NY) + 1;
-  const int nin = grp.in[1] < 0 ? 1 : (grp.in[2] < 0 || !a.aeb ? 2 : 3);
+  const int kind = grp.kind;
+  const int nin = grp.in[1] < 0 ? 1 : (grp.in[2] < 0 || (kind == DG_Q8 && !a.aeb) ? 2 : 3);
+  C* ob = b.W2 + col + grp.out * g.fsc;
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
-    const int bi = k == 0 ? 0 : 1;
+    const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
     const C* in = b.W1 + grp.in[k] * g.fsc + col;
 #pragma unroll 4
     for (int m = 0; m < CL::EPT; m++) {
@@ -463,50 +482,61 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassAr
     }
     __syncthreads();
     fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
-    if (grp.kind == DG_Q8 && k == 1) {  // fold the first two into buffer 0 before the third
-      if (ok) {  // padding columns (kx >= nx/2+1) have no wave numbers
+    if (ok) {
 #pragma unroll 2
-        for (int m = 0; m < CL::EPT; m++) {
-          T ax, ay, az;
-          kfac(K, a.P, pc, rr, kx, x.j(m), 0, ax, ay, az);
-          cx<T> q = -(mul_i(Store<T>::ldc(x.at(0, m)), ax) + mul_i(Store<T>::ldc(x.at(1, m)), ay));
-          Store<T>::stc(x.at(0, m), q);
+      for (int m = 0; m < CL::EPT; m++) {
+        const int ky = x.j(m);
+        T ax, ay, az;
+        kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+        const bool st_ok = g.ky_in(ky);
+        C* o = ob + (long long)ky * g.kxp;
+        cx<T> v0 = Store<T>::ldc(x.at(0, m)), v1 = cx_zero<T>();
+        if (k > 0) v1 = Store<T>::ldc(x.at(1, m));
+        if (kind == DG_Q8) {
+          if (k == 1) {  // fold the two fluxes into buffer 0, unscaled
+            Store<T>::stc(x.at(0, m), -(mul_i(v0, ax) + mul_i(v1, ay)));
+            if (nin == 2 && st_ok) {
+              cx<T> q = -(mul_i(v0, ax) + mul_i(v1, ay));
+              Store<T>::stc(o, {Real<T>::mul_pow2(q.re, sexp), Real<T>::mul_pow2(q.im, sexp)});
+            }
+          } else if (k == 2 && st_ok) {
+            cx<T> q = v0 + v1;
+            Store<T>::stc(o, {Real<T>::mul_pow2(q.re, sexp), Real<T>::mul_pow2(q.im, sexp)});
+          }
+          continue;
+        }
+        v0 = {Real<T>::mul_pow2(v0.re, sexp), Real<T>::mul_pow2(v0.im, sexp)};
+        v1 = {Real<T>::mul_pow2(v1.re, sexp), Real<T>::mul_pow2(v1.im, sexp)};
+        if (!st_ok) continue;
+        switch (kind) {
+          case DG_Q: if (k == 1) Store<T>::stc(o, -(mul_i(v0, ax) + mul_i(v1, ay))); break;
+          case DG_COPY: Store<T>::stc(o, v0); break;
+          case DG_EXY:
+            if (k == 1) {
+              Store<T>::stc(o, v0);
+              Store<T>::stc(o + g.fsc, v1);
+              Store<T>::stc(o + 2 * g.fsc, mul_i(v0, ay) - mul_i(v1, ax));
+            }
+            break;
+          case DG_EZ:
+            Store<T>::stc(o, -mul_i(v0, ay));
+            Store<T>::stc(o + g.fsc, mul_i(v0, ax));
+            break;
+          case DG_QQ:  // buffer 0: Txx then Tyy; buffer 1: Tyx (= Txy)
+            if (k == 1) Store<T>::stc(o, -(mul_i(v0, ax) + mul_i(v1, ay)));
+            else if (k == 2) Store<T>::stc(o + 2 * g.fsc, -(mul_i(v1, ax) + mul_i(v0, ay)));
+            break;
+          default:  // DG_T3: buffer 0: Tzx (= Txz) then Tzz; buffer 1: Tzy (= Tyz)
+            if (k == 0) Store<T>::stc(o, v0);
+            else if (k == 1) {
+              Store<T>::stc(o + 2 * g.fsc, v1);
+              Store<T>::stc(o + 3 * g.fsc, -(mul_i(v0, ax) + mul_i(v1, ay)));
+            } else Store<T>::stc(o + 4 * g.fsc, v0);
+            break;
         }
       }
-      __syncthreads();
     }
-  }
-  if (!ok) return;
-#pragma unroll 2
-  for (int m = 0; m < CL::EPT; m++) {
-    int ky = x.j(m);
-    if (!g.ky_in(ky)) continue;
-    T ax, ay, az;
-    kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
-    cx<T> v0 = Store<T>::ldc(x.at(0, m));
-    v0 = {Real<T>::mul_pow2(v0.re, sexp), Real<T>::mul_pow2(v0.im, sexp)};
-    cx<T> v1 = cx_zero<T>();
-    if (nin > 1) {
-      v1 = Store<T>::ldc(x.at(1, m));
-      v1 = {Real<T>::mul_pow2(v1.re, sexp), Real<T>::mul_pow2(v1.im, sexp)};
-    }
-    C* o = b.W2 + col + (long long)ky * g.kxp + grp.out * g.fsc;
-    switch (grp.kind) {
-      case DG_Q: Store<T>::stc(o, -(mul_i(v0, ax) + mul_i(v1, ay))); break;
-      case DG_COPY: Store<T>::stc(o, v0); break;
-      case DG_EXY:
-        Store<T>::stc(o, v0);
-        Store<T>::stc(o + g.fsc, v1);
-        Store<T>::stc(o + 2 * g.fsc, mul_i(v0, ay) - mul_i(v1, ax));
-        break;
-      case DG_EZ:
-        Store<T>::stc(o, -mul_i(v0, ay));
-        Store<T>::stc(o + g.fsc, mul_i(v0, ax));
-        break;
-      default:  // DG_Q8: buffer 0 holds the folded -(i ax F16 + i ay F17), buffer 1 the expansion term
-        Store<T>::stc(o, nin == 3 ? v0 + v1 : v0);
-        break;
-    }
+    __syncthreads();
   }
 }
 
