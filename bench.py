@@ -40,6 +40,13 @@ WORKLOAD = "3D compressible Hall-MHD + expanding box, 256^3"
 CFG2 = dict(if_resis=1, resistivity=5e-4, if_visc=1, viscosity=5e-4, dealias_option=1, cfl=0.4,
             if_Hall=1, ion_inertial_length=0.05, if_AEB=1, radius0=30.0, Ur0=0.3)
 SHAPE = None  # (nx, ny, nz) of a reduced profiling case
+# --precision: (C-ABI mode, dtype text, state bytes per complex, work-buffer bytes per complex)
+PRECISIONS = {
+    "dd": (1, "f32x2 (float-float)", 16, 16),
+    "fp64": (0, "f64", 16, 16),
+    "fp32": (2, "f32 transforms and products, f32x2 state / RK / CFL / diagnostics", 16, 8),
+    "fp32_f64": (3, "f32 transforms and products, f64 state / RK / CFL / diagnostics", 16, 8),
+}
 PASS_NAMES = ["A_inv_z", "B_inv_y", "C_x_flux", "D_fwd_y", "E_fwd_z_rk", "bookkeeping"]
 
 
@@ -131,19 +138,24 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# algorithmic HBM bytes of one launch of each pass (compulsory reads + writes of the
-# dataflow implemented): S_* are element counts of the touched sub-boxes
-def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, elem=16):
+# algorithmic HBM bytes of one launch of each pass: compulsory reads + writes of the dataflow
+# implemented.  eS / eT are the bytes of one complex element of the state (U, R) and of the work
+# buffers (W1, W2); kx columns are moved in tiles of 8.  Steady-state stages: pruned to the
+# kept modes, continuity taken from the momentum spectrum (mass=True), so pass C transforms 13
+# flux fields (12 without the expansion term) and pass D writes 13 (15 without mass).
+def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, eS=16, eT=16, mass=True):
     kxp8 = int(math.ceil(kx_keep / 8.0) * 8)
     col_A = kxp8 * nky            # columns of pass A / E
     col_B = kxp8 * n              # columns of pass B / D (one per z plane)
-    nin = 8 + (3 if hall else 0)
-    nfl = 18 + (1 if aeb else 0)
-    A = elem * col_A * (8 * nkz + (10 if hall else 8) * n)
-    B = elem * col_B * ((10 if hall else 8) * nky + nin * n)
-    C = elem * n * n * kx_keep * (nin + nfl)
-    D = elem * col_B * (nfl * n + 15 * nky)
-    E = elem * col_A * (15 * n + 8 * nkz * 4)  # read 15 columns; read U, R and write U, R on kept kz
+    na = 10 if hall else 8        # pass A / B outputs (state + current components)
+    nin = 8 + (3 if hall else 0)  # pass C inputs
+    nfl = (13 if mass else 16) - (0 if aeb else 1)
+    nd = 13 if mass else 15
+    A = col_A * (8 * nkz * eS + na * n * eT)
+    B = col_B * (na * nky * eT + nin * n * eT)
+    C = n * n * kx_keep * (nin + nfl) * eT
+    D = col_B * (nfl * n * eT + nd * nky * eT)
+    E = col_A * (nd * n * eT + 8 * nkz * 4 * eS)  # U and R read and written on kept kz
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 
@@ -161,6 +173,35 @@ def cpu_sample(steps, warmup, n=None):
         o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
     el = time.perf_counter() - t0
     return n**3 * steps / el, laps3d._WORKERS, f"{warmup} warm-up + {steps} timed steps at {n}^3 (numpy + scipy.fft pocketfft)"
+
+
+def fp32_error(p, prim, steps):
+    """Per-field relative L2 error and invariant error of an FP32-transform run against the FP64
+    engine after `steps` steps of the same workload (the FP64 engine matches the oracle to
+    1e-10 at these step counts)."""
+    from laps_gb300 import ffi
+
+    out = {}
+    runs = {}
+    for name, mode in (("test", p.precision), ("fp64", ffi.PREC_FP64)):
+        q = ffi.laps_params.from_buffer_copy(p)
+        q.precision = mode
+        r = ffi.Laps(q)
+        r.upload_state(prim, primitive=True)
+        r.set_time(0.0)
+        t, dt, st = r.step(steps)
+        uu, _ = r.download_state()
+        d = r.diagnostics()
+        runs[name] = (uu, np.array([d.e_kin, d.e_mag, d.h_cross, d.h_mag]), t)
+        r.close()
+    a, b = runs["test"], runs["fp64"]
+    rel = [float(np.linalg.norm(a[0][f] - b[0][f]) / max(np.linalg.norm(b[0][f]), 1e-300)) for f in range(8)]
+    out["steps"] = steps
+    out["field_rel_l2"] = rel
+    out["max_field_rel_l2"] = max(rel)
+    out["invariants_rel"] = [float(v) for v in np.abs(a[1] - b[1]) / np.maximum(np.abs(b[1]), 1e-300)]
+    out["time_rel"] = abs(a[2] - b[2]) / b[2]
+    return out
 
 
 def run_reference(args):
@@ -191,7 +232,7 @@ def run_ours(args):
         dist.init_process_group("gloo")
     from laps_gb300 import ffi
 
-    prec = {"dd": ffi.PREC_DD, "fp64": ffi.PREC_FP64}[args.precision]
+    prec = PRECISIONS[args.precision][0]
     n = N_GRID
     prim = initial_state()
     nx, ny, nz = SHAPE if SHAPE else (n, n, n)
@@ -249,7 +290,8 @@ def run_ours(args):
     e2e_ctx.close()
     # ---- roofline of the dominant pass
     nky, nkz = info.ky_keep, info.kz_keep
-    pb = pass_bytes(n, info.kx_keep, nky, nkz) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
+    eS, eT = PRECISIONS[args.precision][2:4]
+    pb = pass_bytes(n, info.kx_keep, nky, nkz, eS=eS, eT=eT) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
     launches = args.steps * 3
     dom = max(range(5), key=lambda i: pass_ms[i])
     name = PASS_NAMES[dom]
@@ -266,7 +308,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32x2 (float-float)" if args.precision == "dd" else "f64",
+        "vs_baseline": None, "dtype": PRECISIONS[args.precision][1],
         "data": "synthetic (seeded random-phase spectrum, 1<=|k|<=8, rms 0.5, seed 1)",
         "config": {"workload": WORKLOAD, "grid": n, "variant": "3DC", "precision": args.precision, "hall": 0.05,
                    "expanding_box": "Ur0/R0=0.01", "dealias": "2/3 sphere", "cfl": 0.4,
@@ -282,6 +324,8 @@ def run_ours(args):
                 "pinned": pinned},
         "clocks": clk.summary(),
     }
+    if args.precision.startswith("fp32") and not SHAPE and not args.no_err:
+        line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
     if rank == 0 and ws == 1 and not args.no_cpu:
         v, cores, sample = cpu_sample(1, 0)
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample}
@@ -302,7 +346,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="dd", choices=["dd", "fp64"])
+    ap.add_argument("--precision", default="dd", choices=list(PRECISIONS))
+    ap.add_argument("--err-steps", type=int, default=10, dest="err_steps",
+                    help="steps of the FP32-vs-FP64 error check of the fp32 modes")
+    ap.add_argument("--no-err", action="store_true", dest="no_err")
     ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
     ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")
     ap.add_argument("--grid", type=int, default=256, help="grid size n (n^3); the headline workload is 256")

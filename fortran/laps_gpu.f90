@@ -8,7 +8,8 @@ module laps_gpu
     integer(c_int), parameter :: LAPS_OK = 0
     integer(c_int), parameter :: LAPS_STATUS_NAN = 1, LAPS_STATUS_DT_FLOOR = 2
     integer(c_int), parameter :: LAPS_VARIANT_3DC = 0, LAPS_VARIANT_3DI = 1, LAPS_VARIANT_2DC = 2
-    integer(c_int), parameter :: LAPS_PREC_FP64 = 0, LAPS_PREC_DD = 1, LAPS_PREC_FP32 = 2
+    integer(c_int), parameter :: LAPS_PREC_FP64 = 0, LAPS_PREC_DD = 1, LAPS_PREC_FP32 = 2, &
+        LAPS_PREC_FP32_F64 = 3
     integer(c_int), parameter :: LAPS_LAYOUT_PRIMITIVE = 0, LAPS_LAYOUT_CONSERVED = 1
 
     type, bind(C) :: laps_params

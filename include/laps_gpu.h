@@ -48,7 +48,8 @@ extern "C" {
 /* arithmetic of the transforms and the right-hand side */
 #define LAPS_PREC_FP64 0 /* native IEEE binary64 everywhere */
 #define LAPS_PREC_DD 1   /* float-float (two FP32, ~48-bit significand) on the FP32 pipes */
-#define LAPS_PREC_FP32 2 /* reserved: FP32 transforms and products */
+#define LAPS_PREC_FP32 2 /* FP32 transforms and products; state, RK update, CFL, diagnostics in float-float */
+#define LAPS_PREC_FP32_F64 3 /* FP32 transforms and products; state, RK update, CFL, diagnostics in FP64 */
 
 /* state layouts for laps_upload_state */
 #define LAPS_LAYOUT_PRIMITIVE 0 /* rho, ux, uy, uz, Bx, By, Bz, p (what outNNN.dat holds) */

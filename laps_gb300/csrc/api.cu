@@ -10,6 +10,10 @@ EngineBase* make_engine_fp64(const laps_params& p);
 EngineBase* make_engine_dd(const laps_params& p);
 long long plan_bytes_fp64(const laps_params& p);
 long long plan_bytes_dd(const laps_params& p);
+EngineBase* make_engine_f32(const laps_params& p);
+long long plan_bytes_f32(const laps_params& p);
+EngineBase* make_engine_f32d(const laps_params& p);
+long long plan_bytes_f32d(const laps_params& p);
 }  // namespace laps
 
 struct laps_ctx {
@@ -70,8 +74,8 @@ int laps_create(const laps_params* p, laps_ctx** out) {
   *out = nullptr;
   if (p->variant != LAPS_VARIANT_3DC && p->variant != LAPS_VARIANT_3DI && p->variant != LAPS_VARIANT_2DC)
     return fail(nullptr, LAPS_EINVAL, "variant must be LAPS_VARIANT_3DC, LAPS_VARIANT_3DI or LAPS_VARIANT_2DC");
-  if (p->precision != LAPS_PREC_FP64 && p->precision != LAPS_PREC_DD)
-    return fail(nullptr, LAPS_EINVAL, "precision must be LAPS_PREC_FP64 or LAPS_PREC_DD");
+  if (p->precision < LAPS_PREC_FP64 || p->precision > LAPS_PREC_FP32_F64)
+    return fail(nullptr, LAPS_EINVAL, "precision must be LAPS_PREC_FP64, LAPS_PREC_DD, LAPS_PREC_FP32 or LAPS_PREC_FP32_F64");
   if (p->variant == LAPS_VARIANT_2DC) {
     if (!size_ok(p->nx, 16) || !size_ok(p->ny, 8) || p->nz != 1)
       return fail(nullptr, LAPS_EINVAL, "2-D: nx a power of two in [16,1024], ny in [8,1024], nz = 1");
@@ -85,13 +89,19 @@ int laps_create(const laps_params* p, laps_ctx** out) {
   if (!(p->Lx > 0 && p->Ly > 0 && p->Lz > 0)) return fail(nullptr, LAPS_EINVAL, "box lengths must be positive");
   if (!(p->adiabatic_index != 1.0) || !(p->cfl > 0)) return fail(nullptr, LAPS_EINVAL, "adiabatic_index must differ from 1 and cfl be positive");
   if (p->if_AEB && !(p->radius0 > 0)) return fail(nullptr, LAPS_EINVAL, "radius0 must be positive");
-  long long need = p->precision == LAPS_PREC_FP64 ? laps::plan_bytes_fp64(*p) : laps::plan_bytes_dd(*p);
+  long long need = p->precision == LAPS_PREC_FP64 ? laps::plan_bytes_fp64(*p)
+                   : p->precision == LAPS_PREC_DD ? laps::plan_bytes_dd(*p)
+                   : p->precision == LAPS_PREC_FP32 ? laps::plan_bytes_f32(*p)
+                                                    : laps::plan_bytes_f32d(*p);
   if (p->mem_cap_bytes > 0 && need > p->mem_cap_bytes)
     return fail(nullptr, LAPS_ENOMEM, "device memory needed (" + std::to_string(need) + " bytes) exceeds mem_cap_bytes");
   laps_ctx* c = new (std::nothrow) laps_ctx;
   if (!c) return fail(nullptr, LAPS_ENOMEM, "host allocation failed");
   try {
-    c->e = p->precision == LAPS_PREC_FP64 ? laps::make_engine_fp64(*p) : laps::make_engine_dd(*p);
+    c->e = p->precision == LAPS_PREC_FP64 ? laps::make_engine_fp64(*p)
+           : p->precision == LAPS_PREC_DD ? laps::make_engine_dd(*p)
+           : p->precision == LAPS_PREC_FP32 ? laps::make_engine_f32(*p)
+                                            : laps::make_engine_f32d(*p);
   } catch (const laps::Error& e) {
     delete c;
     return fail(nullptr, e.code, e.msg);

@@ -205,4 +205,24 @@ template <> struct Store<float> {
   __device__ __forceinline__ static void stc(C* p, cx<float> v) { *p = make_float2(v.re, v.im); }
 };
 
+// ------------------------------------------------------------------------------ conversions
+// between the compute type of the transforms and the storage type of the state
+template <class D, class S> struct Cvt;
+template <class T> struct Cvt<T, T> {
+  __device__ __forceinline__ static T r(T x) { return x; }
+};
+template <> struct Cvt<float, dd> {  // nearest float of hi + lo
+  __device__ __forceinline__ static float r(dd x) { return __fadd_rn(x.hi, x.lo); }
+};
+template <> struct Cvt<dd, float> {
+  __device__ __forceinline__ static dd r(float x) { return {x, 0.f}; }
+};
+template <> struct Cvt<float, double> {
+  __device__ __forceinline__ static float r(double x) { return __double2float_rn(x); }
+};
+template <> struct Cvt<double, float> {
+  __device__ __forceinline__ static double r(float x) { return (double)x; }
+};
+template <class D, class S> __device__ __forceinline__ cx<D> cvtc(cx<S> v) { return {Cvt<D, S>::r(v.re), Cvt<D, S>::r(v.im)}; }
+
 }  // namespace laps

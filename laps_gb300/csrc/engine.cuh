@@ -82,6 +82,14 @@ template <class T> struct PT {
   T ebm[8];          // expansion damping factor of each variable
 };
 
+// everything a pass needs in the compute type T and in the state type TS
+template <class T, class TS> struct PassK {
+  PT<T> pc;
+  PT<TS> ps;
+  KTab<T> K;
+  KTab<TS> KS;
+};
+
 // effective derivative factors (i*ax, i*ay, i*az) at spectral index (ix, iy, iz):
 // src_compressible/mhdrhs.f90:191-204 (corotation mixes kx and ky)
 template <class T>

@@ -61,15 +61,20 @@ class EngineBase {
   virtual void step_profiled(int n, double* pass_ms, double* total_ms, int* status) = 0;
 };
 
-template <class T> class Engine : public EngineBase {
+// T: compute type of the transforms and products; TS: storage type of the state, the RK
+// register, the CFL arithmetic and the diagnostics (equal except in the FP32-transform mode)
+template <class T, class TS = T> class Engine : public EngineBase {
   using C = typename Store<T>::C;
   using SR = typename Store<T>::R;
+  using CS = typename Store<TS>::C;
+  using SRS = typename Store<TS>::R;
 
  public:
   laps_params p;
   Geo gfull, gprune;
   Phys P;
   PT<T> pc;
+  PT<TS> ps;
   bool prune_ok = false;   // dealias option 1: the box |k_i| <= n_i/3 holds every non-zero mode
   bool dealiased = false;  // the state has been through at least one RK stage since upload
   bool have_state = false;
@@ -78,8 +83,10 @@ template <class T> class Engine : public EngineBase {
   cudaGraphExec_t graph_steady = nullptr;
   long long bytes = 0;
   std::vector<void*> allocs;
-  Bufs<T> B{};
-  C *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  Bufs<T, TS> B{};
+  C *twx = nullptr, *twy = nullptr, *twz = nullptr;      // twiddles in T (passes)
+  CS *twxs = nullptr, *twys = nullptr, *twzs = nullptr;  // twiddles in TS (state transforms)
+  SRS *s_wx, *s_kxd, *s_wy, *s_kyd, *s_kzd, *s_kx2, *s_ky2, *s_kz2, *s_fx = nullptr, *s_fy = nullptr, *s_fz = nullptr;
   SR *t_wx, *t_kxd, *t_wy, *t_kyd, *t_kzd, *t_kx2, *t_ky2, *t_kz2, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr;
   double *d_wx, *d_wy, *d_wz;
   short* kxlim = nullptr;
@@ -96,10 +103,26 @@ template <class T> class Engine : public EngineBase {
   }
 
   static int w2_fields(const laps_params& q) { return q.variant == LAPS_VARIANT_3DI ? 19 : 15; }
+  // work buffers also stage state-type data (upload, download, diagnostics)
+  static constexpr long long WE = sizeof(C) > sizeof(CS) ? sizeof(C) : sizeof(CS);
   static long long plan_bytes(const laps_params& q) {
     long long kxp = ((q.nx / 2 + 1) + 7) / 8 * 8;
     long long fsc = kxp * q.ny * q.nz;
-    return (8 + 8 + 19 + w2_fields(q)) * fsc * (long long)sizeof(C) + (1 << 20);
+    return (8 + 8) * fsc * (long long)sizeof(CS) + (19 + w2_fields(q)) * fsc * WE + (1 << 20);
+  }
+  template <class X> static PT<X> make_pt(const Phys& P) {
+    PT<X> c;
+    c.gamma = host_cvt<X>(P.gamma); c.gm1 = host_cvt<X>(P.gamma - 1.0);
+    c.cg = host_cvt<X>(-2.0 * P.gamma / (P.gamma - 1.0));
+    c.di = host_cvt<X>(P.di); c.nu = host_cvt<X>(P.nu); c.eta = host_cvt<X>(P.eta);
+    c.cosc = host_cvt<X>(P.cos_cor); c.sinc = host_cvt<X>(P.sin_cor);
+    c.inv_mindx = host_cvt<X>(1.0 / P.mindx);
+    c.half = host_cvt<X>(0.5); c.two = host_cvt<X>(2.0); c.one = host_cvt<X>(1.0);
+    c.zero = host_cvt<X>(0.0); c.four = host_cvt<X>(4.0);
+    c.is2 = host_cvt<X>(0.70710678118654752440L);
+    c.dx = host_cvt<X>(P.dx); c.dy = host_cvt<X>(P.dy); c.dz = host_cvt<X>(P.dz);
+    c.eta_dx = host_cvt<X>(P.eta / P.dx); c.eta_dy = host_cvt<X>(P.eta / P.dy);
+    return c;
   }
 
   explicit Engine(const laps_params& q) : p(q) {
@@ -130,23 +153,18 @@ template <class T> class Engine : public EngineBase {
     P.dealias = (q.dealias_option == 1 || q.dealias_option == 2 || (two_d && q.dealias_option == 3)) ? q.dealias_option : 0;
     P.variant = q.variant; P.two_d = two_d; P.zrad = two_d && q.if_AEB && q.if_z_radial;
     P.limit_dt = two_d && q.if_limit_dt_increase; P.dstep = two_d ? q.dstep_calcdt : 1;
-    pc.gamma = host_cvt<T>(P.gamma); pc.gm1 = host_cvt<T>(P.gamma - 1.0);
-    pc.cg = host_cvt<T>(-2.0 * P.gamma / (P.gamma - 1.0));
-    pc.di = host_cvt<T>(P.di); pc.nu = host_cvt<T>(P.nu); pc.eta = host_cvt<T>(P.eta);
-    pc.cosc = host_cvt<T>(P.cos_cor); pc.sinc = host_cvt<T>(P.sin_cor);
-    pc.inv_mindx = host_cvt<T>(1.0 / P.mindx);
-    pc.half = host_cvt<T>(0.5); pc.two = host_cvt<T>(2.0); pc.one = host_cvt<T>(1.0);
-    pc.zero = host_cvt<T>(0.0); pc.four = host_cvt<T>(4.0);
-    pc.is2 = host_cvt<T>(0.70710678118654752440L);
-    pc.dx = host_cvt<T>(P.dx); pc.dy = host_cvt<T>(P.dy); pc.dz = host_cvt<T>(P.dz);
-    pc.eta_dx = host_cvt<T>(P.eta / P.dx); pc.eta_dy = host_cvt<T>(P.eta / P.dy);
+    pc = make_pt<T>(P);
+    ps = make_pt<TS>(P);
     // expansion damping of each variable: mhdrhs.f90:237-247; 2D/mhdrhs.f90:319-343 (radial z);
     // src_incompressible/mhdrhs.f90:187-204 (p decays with 2 gamma)
     double ebm[8] = {2.0, 2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 0.0};
     if (P.zrad) { double zr[8] = {2.0, 3.0, 3.0, 2.0, 1.0, 1.0, 2.0, 0.0}; std::memcpy(ebm, zr, sizeof ebm); }
     if (incomp) ebm[7] = 2.0 * P.gamma;
     P.ebm_mask = incomp ? 0xFF : 0x7F;
-    for (int v = 0; v < 8; v++) pc.ebm[v] = host_cvt<T>(ebm[v]);
+    for (int v = 0; v < 8; v++) {
+      pc.ebm[v] = host_cvt<T>(ebm[v]);
+      ps.ebm[v] = host_cvt<TS>(ebm[v]);
+    }
 
     // wave numbers, mhdinit.f90:88-115 (the Nyquist index takes +k)
     auto wn = [&](int n, double L) {
@@ -197,13 +215,13 @@ template <class T> class Engine : public EngineBase {
     }
 
     LAPS_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    B.U = dalloc<C>(8 * g.fsc);
-    B.R = dalloc<C>(8 * g.fsc);
-    B.W1 = dalloc<C>(19 * g.fsc);
-    B.W2 = dalloc<C>(w2_fields(q) * g.fsc);
-    bytes = (8 + 8 + 19 + w2_fields(q)) * g.fsc * (long long)sizeof(C);
-    LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(C), stream));
-    LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
+    B.U = dalloc<CS>(8 * g.fsc);
+    B.R = dalloc<CS>(8 * g.fsc);
+    B.W1 = (C*)dalloc<unsigned char>(19 * g.fsc * WE);
+    B.W2 = (C*)dalloc<unsigned char>(w2_fields(q) * g.fsc * WE);
+    bytes = plan_bytes(q) - (1 << 20);
+    LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
+    LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(CS), stream));
     auto up = [&](auto* dst, const auto& src) {
       LAPS_CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
     };
@@ -211,29 +229,42 @@ template <class T> class Engine : public EngineBase {
     twx = dalloc<C>(q.nx); up(twx, twx_h);
     twy = dalloc<C>(q.ny); up(twy, twy_h);
     twz = dalloc<C>(q.nz); up(twz, twz_h);
+    auto twxs_h = twiddles<TS>(q.nx), twys_h = twiddles<TS>(q.ny), twzs_h = twiddles<TS>(q.nz);
+    twxs = dalloc<CS>(q.nx); up(twxs, twxs_h);
+    twys = dalloc<CS>(q.ny); up(twys, twys_h);
+    twzs = dalloc<CS>(q.nz); up(twzs, twzs_h);
     d_wx = dalloc<double>(g.nh); up(d_wx, wx);
     d_wy = dalloc<double>(q.ny); up(d_wy, wy);
     d_wz = dalloc<double>(q.nz); up(d_wz, wz);
     t_wx = dalloc<SR>(g.nh); t_kxd = dalloc<SR>(g.nh); t_kx2 = dalloc<SR>(g.nh);
     t_wy = dalloc<SR>(q.ny); t_kyd = dalloc<SR>(q.ny); t_ky2 = dalloc<SR>(q.ny);
     t_kzd = dalloc<SR>(q.nz); t_kz2 = dalloc<SR>(q.nz);
+    s_wx = dalloc<SRS>(g.nh); s_kxd = dalloc<SRS>(g.nh); s_kx2 = dalloc<SRS>(g.nh);
+    s_wy = dalloc<SRS>(q.ny); s_kyd = dalloc<SRS>(q.ny); s_ky2 = dalloc<SRS>(q.ny);
+    s_kzd = dalloc<SRS>(q.nz); s_kz2 = dalloc<SRS>(q.nz);
     if (P.dealias == 1 || P.dealias == 3) { kxlim = dalloc<short>(lim.size()); up(kxlim, lim); }
     if (P.dealias == 2) {  // dealiasing.f90:31-65
-      auto filt = [&](const std::vector<double>& w, double L, int n, double af) {
+      auto filt = [&](auto tag, const std::vector<double>& w, double L, int n, double af) {
+        using X = decltype(tag);
+        using XR = typename Store<X>::R;
         double aj = (5.0 + 6.0 * af) / 8.0, bj = (1.0 + 2.0 * af) / 2.0, cj = -(1.0 - 2 * af) / 8.0;
-        std::vector<SR> f(w.size());
+        std::vector<XR> f(w.size());
         for (size_t i = 0; i < w.size(); i++) {
           double wl = w[i] * L / n;
           double v = (aj + bj * std::cos(wl) + cj * std::cos(2 * wl)) / (1 + 2 * af * std::cos(wl));
-          T tv = host_cvt<T>(v);
-          std::memcpy(&f[i], &tv, sizeof(SR));
+          X tv = host_cvt<X>(v);
+          std::memcpy(&f[i], &tv, sizeof(XR));
         }
         return f;
       };
-      auto fx = filt(wx, q.Lx, q.nx, q.afx), fy = filt(wy, q.Ly, q.ny, q.afy), fz = filt(wz, q.Lz, q.nz, q.afz);
+      auto fx = filt(T{}, wx, q.Lx, q.nx, q.afx), fy = filt(T{}, wy, q.Ly, q.ny, q.afy), fz = filt(T{}, wz, q.Lz, q.nz, q.afz);
       t_fx = dalloc<SR>(fx.size()); up(t_fx, fx);
       t_fy = dalloc<SR>(fy.size()); up(t_fy, fy);
       t_fz = dalloc<SR>(fz.size()); up(t_fz, fz);
+      auto gx = filt(TS{}, wx, q.Lx, q.nx, q.afx), gy = filt(TS{}, wy, q.Ly, q.ny, q.afy), gz = filt(TS{}, wz, q.Lz, q.nz, q.afz);
+      s_fx = dalloc<SRS>(gx.size()); up(s_fx, gx);
+      s_fy = dalloc<SRS>(gy.size()); up(s_fy, gy);
+      s_fz = dalloc<SRS>(gz.size()); up(s_fz, gz);
     }
     if ((P.dealias == 1 || P.dealias == 3) && !kxlim) throw Error{LAPS_EINVAL, "dealias table missing"};
     if (P.dealias == 2 && !(t_fx && t_fy && t_fz)) throw Error{LAPS_EINVAL, "dealias filters missing"};
@@ -271,38 +302,56 @@ template <class T> class Engine : public EngineBase {
     return K;
   }
 
+  KTab<TS> ktab_s() const {
+    KTab<TS> K;
+    K.wx = (const TS*)s_wx; K.kxd = (const TS*)s_kxd; K.wy = (const TS*)s_wy; K.kyd = (const TS*)s_kyd; K.kzd = (const TS*)s_kzd;
+    K.kx2 = (const TS*)s_kx2; K.ky2 = (const TS*)s_ky2; K.kz2 = (const TS*)s_kz2;
+    K.fx = (const TS*)s_fx; K.fy = (const TS*)s_fy; K.fz = (const TS*)s_fz;
+    K.kxlim = kxlim;
+    return K;
+  }
+  PassK<T, TS> passk() const { return PassK<T, TS>{pc, ps, ktab(), ktab_s()}; }
+
   void tables() {
     k_tables<T><<<1, 256, 0, stream>>>(d_wx, d_wy, d_wz, t_wx, t_kxd, t_wy, t_kyd, t_kzd, t_kx2, t_ky2, t_kz2, gfull.nh, p.ny,
                                        p.nz, p.radius0, P.zrad, st);
     LAPS_CK(cudaGetLastError());
+    k_tables<TS><<<1, 256, 0, stream>>>(d_wx, d_wy, d_wz, s_wx, s_kxd, s_wy, s_kyd, s_kzd, s_kx2, s_ky2, s_kz2, gfull.nh, p.ny,
+                                        p.nz, p.radius0, P.zrad, st);
+    LAPS_CK(cudaGetLastError());
   }
 
   // ---------------------------------------------------------------- plain transforms
-  void col_plain(const C* in, C* out, int nf, int N, int dir, int jstride, int ostride, int ncol, int nouter, int sexp,
-                 const C* tw) {
-    launch_col_plain<T>(stream, in, out, gfull.fsc, nf, N, dir, jstride, ostride, ncol, nouter, sexp, tw);
+  // plain transforms of state-type data; the work buffers are reused as state-type arrays
+  CS* W1s() const { return (CS*)B.W1; }
+  CS* W2s() const { return (CS*)B.W2; }
+  void col_plain(const CS* in, CS* out, int nf, int N, int dir, int jstride, int ostride, int ncol, int nouter, int sexp,
+                 const CS* tw) {
+    launch_col_plain<TS>(stream, in, out, gfull.fsc, nf, N, dir, jstride, ostride, ncol, nouter, sexp, tw);
   }
-  void rows_r2c(const SR* in, C* out, long long nrows) { launch_rows_r2c<T>(stream, p.nx, in, out, nrows, gfull.kxp, twx); }
-  void rows_c2r(const C* in, SR* out, long long nrows) { launch_rows_c2r<T>(stream, p.nx, in, out, nrows, gfull.kxp, twx); }
-  // real T fields (W1 layout, nf) -> spectrum `out` (fsc pitch)
-  void forward3d(const SR* real, C* out, int nf) {
+  void rows_r2c(const SRS* in, CS* out, long long nrows) { launch_rows_r2c<TS>(stream, p.nx, in, out, nrows, gfull.kxp, twxs); }
+  void rows_c2r(const CS* in, SRS* out, long long nrows) { launch_rows_c2r<TS>(stream, p.nx, in, out, nrows, gfull.kxp, twxs); }
+  // real TS fields (W1 layout, nf) -> spectrum `out` (fsc pitch)
+  void forward3d(const SRS* real, CS* out, int nf) {
     const Geo& g = gfull;
-    rows_r2c(real, B.W2, (long long)nf * g.ny * g.nz);
+    CS* w2 = W2s();
+    rows_r2c(real, w2, (long long)nf * g.ny * g.nz);
     for (int f = 0; f < nf; f++) {
       // y: element (f, z, y, kx): jstride = kxp, outer = z with ostride ny*kxp
-      col_plain(B.W2 + f * g.fsc, B.W2 + f * g.fsc, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twy);
+      col_plain(w2 + f * g.fsc, w2 + f * g.fsc, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twys);
       // z: jstride = ny*kxp, outer = y with ostride kxp
-      col_plain(B.W2 + f * g.fsc, out + f * g.fsc, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twz);
+      col_plain(w2 + f * g.fsc, out + f * g.fsc, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twzs);
     }
   }
-  // spectrum (nf fields) -> real T fields in W1
-  void inverse3d(const C* spec, int nf) {
+  // spectrum (nf fields) -> real TS fields in W1
+  void inverse3d(const CS* spec, int nf) {
     const Geo& g = gfull;
+    CS* w2 = W2s();
     for (int f = 0; f < nf; f++) {
-      col_plain(spec + f * g.fsc, B.W2 + f * g.fsc, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twz);
-      col_plain(B.W2 + f * g.fsc, B.W2 + f * g.fsc, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twy);
+      col_plain(spec + f * g.fsc, w2 + f * g.fsc, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twzs);
+      col_plain(w2 + f * g.fsc, w2 + f * g.fsc, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twys);
     }
-    rows_c2r(B.W2, (SR*)B.W1, (long long)nf * g.ny * g.nz);
+    rows_c2r(w2, (SRS*)B.W1, (long long)nf * g.ny * g.nz);
   }
 
   // ---------------------------------------------------------------- fused passes
@@ -310,15 +359,16 @@ template <class T> class Engine : public EngineBase {
     PassArgs a;
     a.g = g; a.P = P; a.hall = P.hall; a.aeb = P.aeb; a.stage = stage; a.store_rk = store_rk; a.cfl = cfl; a.st = st;
     a.mass_from_state = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
+    a.e_first = 0;
     return a;
   }
-  void passA(const PassArgs& a) { launch_passA<T>(stream, p.nz, B, a, pc, ktab(), twz); }
-  void passB(const PassArgs& a) { launch_passB<T>(stream, p.ny, B, a, pc, ktab(), twy); }
-  void passC(const PassArgs& a) { launch_passC<T>(stream, p.nx, B, a, pc, twx); }
-  void passD(const PassArgs& a) { launch_passD<T>(stream, p.ny, B, a, pc, ktab(), twy); }
+  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz); }
+  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy); }
+  void passC(const PassArgs& a) { launch_passC<T, TS>(stream, p.nx, B, a, passk(), twx); }
+  void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy); }
   void passE(const PassArgs& a) {
-    if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T>(stream, p.nz, B, a, pc, ktab(), twz);
-    else launch_passE<T>(stream, p.nz, B, a, pc, ktab(), twz);
+    if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T, TS>(stream, p.nz, B, a, passk(), twz);
+    else launch_passE<T, TS>(stream, p.nz, B, a, passk(), twz);
   }
 
   // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage
@@ -435,10 +485,10 @@ template <class T> class Engine : public EngineBase {
     const Geo& g = gfull;
     double* stage = (double*)B.W2;  // 8 real float64 fields fit in 15 complex fields
     LAPS_CK(cudaMemcpyAsync(stage, h, 8 * g.fsr * sizeof(double), cudaMemcpyHostToDevice, stream));
-    k_upload_convert<T><<<1024, 256, 0, stream>>>(stage, (SR*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma,
-                                                  P.variant == LAPS_VARIANT_3DI);
+    k_upload_convert<TS><<<1024, 256, 0, stream>>>(stage, (SRS*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma,
+                                                   P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
-    forward3d((const SR*)B.W1, B.U, 8);
+    forward3d((const SRS*)B.W1, B.U, 8);
     // mhd.f90:135: dt = 0 before the first vardt, so the first CFL value is taken as is
     LAPS_CK(cudaMemsetAsync(&st->dt, 0, sizeof(double), stream));
     dealiased = false;
@@ -508,8 +558,8 @@ template <class T> class Engine : public EngineBase {
     const Geo& g = gfull;
     inverse3d(B.U, 8);
     double* out = (double*)B.W2;  // 12 real float64 fields fit in 15 complex fields
-    k_download_convert<T><<<1024, 256, 0, stream>>>((const SR*)B.W1, uu ? out : nullptr, prim ? out + 8 * g.fsr : nullptr,
-                                                    g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI);
+    k_download_convert<TS><<<1024, 256, 0, stream>>>((const SRS*)B.W1, uu ? out : nullptr, prim ? out + 8 * g.fsr : nullptr,
+                                                     g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     if (uu) LAPS_CK(cudaMemcpyAsync(uu, out, 8 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
     if (prim) LAPS_CK(cudaMemcpyAsync(prim, out + 8 * g.fsr, 4 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -518,7 +568,7 @@ template <class T> class Engine : public EngineBase {
   void download_spectral(double* uf) override {
     const Geo& g = gfull;
     double2* out = (double2*)B.W1;
-    k_spec_to_ref<T><<<1024, 256, 0, stream>>>(B.U, out, g, 8);
+    k_spec_to_ref<TS><<<1024, 256, 0, stream>>>(B.U, out, g, 8);
     LAPS_CK(cudaGetLastError());
     LAPS_CK(cudaMemcpyAsync(uf, out, (size_t)8 * g.nz * g.ny * g.nh * sizeof(double2), cudaMemcpyDeviceToHost, stream));
     wait(tmo());
@@ -527,7 +577,7 @@ template <class T> class Engine : public EngineBase {
     const Geo& g = gfull;
     double2* in = (double2*)B.W1;
     LAPS_CK(cudaMemcpyAsync(in, uf, (size_t)8 * g.nz * g.ny * g.nh * sizeof(double2), cudaMemcpyHostToDevice, stream));
-    k_spec_from_ref<T><<<1024, 256, 0, stream>>>(in, B.U, g, 8);
+    k_spec_from_ref<TS><<<1024, 256, 0, stream>>>(in, B.U, g, 8);
     LAPS_CK(cudaGetLastError());
     dealiased = false;
     have_state = true;
@@ -544,13 +594,16 @@ template <class T> class Engine : public EngineBase {
     i->kx_keep = gprune.kx_keep;
     i->ky_keep = gprune.nky();
     i->kz_keep = gprune.nkz();
-    i->kernels_per_step = 3 * (P.two_d ? 4 : 5) + 3;
+    // per stage: passes A (3-D), B, C, D, E (E in two launches when the continuity term comes
+    // from the momentum); per step: dt finalisation, time advance, two table updates
+    const bool mass = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
+    i->kernels_per_step = 3 * ((P.two_d ? 4 : 5) + (mass ? 1 : 0)) + 4;
     i->graph = graph_steady != nullptr;
   }
 };
 
 // ---------------------------------------------------------------------------- diagnostics
-template <class T> void Engine<T>::diagnostics(laps_diag* d) {
+template <class T, class TS> void Engine<T, TS>::diagnostics(laps_diag* d) {
   if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
   const Geo& g = gfull;
   read_state();
@@ -560,7 +613,7 @@ template <class T> void Engine<T>::diagnostics(laps_diag* d) {
   inverse3d(B.U, 8);  // real conserved T fields in W1
   int nb = npart;
   // pass 1: sums of f and f^2 for the 8 reported fields, the energies and u.B
-  k_diag_sums<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI, d_part);
+  k_diag_sums<TS><<<nb, 256, 0, stream>>>((const SRS*)B.W1, g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI, d_part);
   LAPS_CK(cudaGetLastError());
   std::vector<double> part((size_t)nb * 32);
   LAPS_CK(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -579,10 +632,10 @@ template <class T> void Engine<T>::diagnostics(laps_diag* d) {
   d->e_mag = 0.5 * s[17] / n;
   d->h_cross = s[18] / n;
   // pass 2: rho (u - <u>)^2
-  k_diag_rhou2<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, ave[1], ave[2], ave[3], d_part);
+  k_diag_rhou2<TS><<<nb, 256, 0, stream>>>((const SRS*)B.W1, g.fsr, ave[1], ave[2], ave[3], d_part);
   LAPS_CK(cudaGetLastError());
   // spectral: max |ik.B| and <A.B>
-  k_diag_spec<T><<<nb, 256, 0, stream>>>(B.U, g, ktab(), P, pc, st, d_part + (size_t)nb * 8);
+  k_diag_spec<TS><<<nb, 256, 0, stream>>>(B.U, g, ktab_s(), P, ps, st, d_part + (size_t)nb * 8);
   LAPS_CK(cudaGetLastError());
   LAPS_CK(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
   wait(tmo());
@@ -598,11 +651,11 @@ template <class T> void Engine<T>::diagnostics(laps_diag* d) {
   // real-space maxima of div B and div(rho u)/rho0 (the incompressible code's diagnostics)
   double mreal[2];
   for (int w = 0; w < 2; w++) {
-    C* spec = B.W2 + (w2_fields(p) - 1) * g.fsc;
-    k_spec_div<T><<<1024, 256, 0, stream>>>(B.U, spec, g, ktab(), P, pc, st, w == 0 ? 4 : 1, w == 1);
+    CS* spec = W2s() + (w2_fields(p) * WE / (long long)sizeof(CS) - 1) * g.fsc;
+    k_spec_div<TS><<<1024, 256, 0, stream>>>(B.U, spec, g, ktab_s(), P, ps, st, w == 0 ? 4 : 1, w == 1);
     LAPS_CK(cudaGetLastError());
     inverse3d(spec, 1);
-    k_max_abs<T><<<nb, 256, 0, stream>>>((const SR*)B.W1, g.fsr, d_part);
+    k_max_abs<TS><<<nb, 256, 0, stream>>>((const SRS*)B.W1, g.fsr, d_part);
     LAPS_CK(cudaGetLastError());
     LAPS_CK(cudaMemcpyAsync(part.data(), d_part, (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, stream));
     wait(tmo());

@@ -30,12 +30,14 @@ template <class T, int N> struct Col {
   static constexpr int SMEM = NTILE * N * TX * (int)sizeof(C);  // one buffer per tile
 };
 
-template <class T> struct Bufs {
-  using C = typename Store<T>::C;
-  C* U;   // state spectrum, 8 fields
-  C* R;   // fnl_rk, 8 fields
-  C* W1;  // work, up to 19 fields
-  C* W2;  // work, up to 15 fields
+// T: the compute type of the transforms and products; TS: the storage type of the state
+// and of the RK register (the same except in the FP32-transform mode, where TS is
+// float-float)
+template <class T, class TS = T> struct Bufs {
+  typename Store<TS>::C* U;  // state spectrum, 8 fields
+  typename Store<TS>::C* R;  // fnl_rk, 8 fields
+  typename Store<T>::C* W1;  // work, up to 19 fields
+  typename Store<T>::C* W2;  // work, up to 19 fields
 };
 
 // --------------------------------------------------------------------------- plain transforms
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(Col<T, N>::THREADS)
 #pragma unroll 4
   for (int m = 0; m < CL::EPT; m++) {
     int j = t + m * CL::TPL;
-    cx<T> v = ok ? Store<T>::ldg(in + base + (long long)j * jstride) : cx_zero<T>();
+    cx<T> v = ok ? Store<T>::ldc(in + base + (long long)j * jstride) : cx_zero<T>();  // in may equal out
     Store<T>::stc(s + j * TX + c, v);
   }
   __syncthreads();

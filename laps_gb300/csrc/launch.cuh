@@ -37,21 +37,22 @@ void launch_rows_r2c(cudaStream_t stream, int nx, const typename Store<T>::R* in
 template <class T>
 void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in, typename Store<T>::R* out, long long nrows, int kxp,
                      const typename Store<T>::C* twx);
-template <class T> void launch_passA(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
-template <class T> void launch_passB(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
-template <class T, int INCOMP, int CFL>
-void launch_passC_v(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw);
-template <class T> void launch_passC(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
+template <class T, class TS> void launch_passA(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passB(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS, int INCOMP, int CFL>
+void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS>
+void launch_passC(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw) {
   if (a.P.variant == LAPS_VARIANT_3DI) {
-    if (a.cfl) launch_passC_v<T, 1, 1>(stream, N, B, a, pc, tw);
-    else launch_passC_v<T, 1, 0>(stream, N, B, a, pc, tw);
+    if (a.cfl) launch_passC_v<T, TS, 1, 1>(stream, N, B, a, kk, tw);
+    else launch_passC_v<T, TS, 1, 0>(stream, N, B, a, kk, tw);
   } else {
-    if (a.cfl) launch_passC_v<T, 0, 1>(stream, N, B, a, pc, tw);
-    else launch_passC_v<T, 0, 0>(stream, N, B, a, pc, tw);
+    if (a.cfl) launch_passC_v<T, TS, 0, 1>(stream, N, B, a, kk, tw);
+    else launch_passC_v<T, TS, 0, 0>(stream, N, B, a, kk, tw);
   }
 }
-template <class T> void launch_passD(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
-template <class T> void launch_passE(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
-template <class T> void launch_passE3i(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passD(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passE(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passE3i(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
 
 }  // namespace laps

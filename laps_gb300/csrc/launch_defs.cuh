@@ -56,18 +56,18 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
 }
 
 #define LAPS_COL_PASS(NAME, KERNEL, NOUTER)                                                                              \
-  template <class T>                                                                                                    \
-  void NAME(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* tw) {    \
+  template <class T, class TS>                                                                                          \
+  void NAME(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw) {  \
     switch (N) { LAPS_COL_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported line length"}; }               \
     LAPS_CK(cudaGetLastError());                                                                                        \
   }
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passA<T, NN>, CL::SMEM);                                                                                 \
+    set_smem(k_passA<T, TS, NN>, CL::SMEM);                                                                                 \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE,                                     \
               a.P.variant == LAPS_VARIANT_3DI ? 12 : (a.hall ? 10 : 8));                                                \
-    k_passA<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    k_passA<T, TS, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, kk, tw);                                           \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passA, k_passA, nky)
@@ -75,10 +75,10 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passB<T, NN>, CL::SMEM);                                                                                 \
+    set_smem(k_passB<T, TS, NN>, CL::SMEM);                                                                                 \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
-    k_passB<T, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, pc, K, tw);                                           \
+    k_passB<T, TS, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, kk, tw);                                           \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passB, k_passB, nz)
@@ -86,9 +86,9 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passD<T, NN>, 2 * CL::SMEM);                                                                             \
+    set_smem(k_passD<T, TS, NN>, 2 * CL::SMEM);                                                                             \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : (a.mass_from_state ? 6 : 8)); \
-    k_passD<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
+    k_passD<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw);                                       \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passD, k_passD, nz)
@@ -96,9 +96,17 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passE<T, NN>, 2 * CL::SMEM);                                                                             \
+    set_smem(k_passE<T, TS, NN>, 2 * CL::SMEM);                                                                         \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, 8);                                  \
-    k_passE<T, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                       \
+    PassArgs a0 = a;                                                                                                    \
+    a0.e_first = 0;                                                                                                     \
+    if (a.mass_from_state) { /* continuity from the momentum first, then variables 1..7 */                             \
+      grid.z = 1;                                                                                                       \
+      k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw);                                   \
+      a0.e_first = 1;                                                                                                   \
+      grid.z = 7;                                                                                                       \
+    }                                                                                                                   \
+    k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw);                                     \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passE, k_passE, nky)
@@ -106,9 +114,9 @@ LAPS_COL_PASS(launch_passE, k_passE, nky)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passE3i<T, NN>, 3 * CL::SMEM);                                                                           \
+    set_smem(k_passE3i<T, TS, NN>, 3 * CL::SMEM);                                                                           \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE, 4);                                  \
-    k_passE3i<T, NN><<<grid, CL::THREADS, 3 * CL::SMEM, stream>>>(B, a, pc, K, tw);                                     \
+    k_passE3i<T, TS, NN><<<grid, CL::THREADS, 3 * CL::SMEM, stream>>>(B, a, kk, tw);                                     \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passE3i, k_passE3i, nky)
@@ -117,14 +125,14 @@ LAPS_COL_PASS(launch_passE3i, k_passE3i, nky)
 
 // pass C for one (physics, CFL) combination; each combination is instantiated in its own
 // translation unit (launch_passC_<type>_<c|i><0|1>.cu)
-template <class T, int INCOMP, int CFL>
-void launch_passC_v(cudaStream_t stream, int N, Bufs<T> B, PassArgs a, PT<T> pc, const typename Store<T>::C* tw) {
+template <class T, class TS, int INCOMP, int CFL>
+void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw) {
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CF = PassCCfg<NN>;                                                                                            \
     unsigned nb = (unsigned)((long long)a.g.ny * a.g.nz / CF::ROWS);                                                    \
-    set_smem(k_passC<T, NN, CFL, INCOMP>, CF::SMEM);                                                                    \
-    k_passC<T, NN, CFL, INCOMP><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, pc, tw);                                   \
+    set_smem(k_passC<T, TS, NN, CFL, INCOMP>, CF::SMEM);                                                                \
+    k_passC<T, TS, NN, CFL, INCOMP><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, kk, tw);                               \
     break;                                                                                                              \
   }
   switch (N) { LAPS_ROW_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported nx"}; }

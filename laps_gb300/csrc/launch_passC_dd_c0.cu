@@ -1,5 +1,5 @@
-// Pass C launcher (dd, compressible, CFL 0).
+// Pass C launcher (dd transforms, dd state, compressible, CFL 0).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passC_v<dd, 0, 0>(cudaStream_t, int, Bufs<dd>, PassArgs, PT<dd>, const Store<dd>::C*);
+template void launch_passC_v<dd, dd, 0, 0>(cudaStream_t, int, Bufs<dd, dd>, PassArgs, PassK<dd, dd>, const Store<dd>::C*);
 }  // namespace laps

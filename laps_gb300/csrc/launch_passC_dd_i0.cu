@@ -1,5 +1,5 @@
-// Pass C launcher (dd, incompressible, CFL 0).
+// Pass C launcher (dd transforms, dd state, incompressible, CFL 0).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passC_v<dd, 1, 0>(cudaStream_t, int, Bufs<dd>, PassArgs, PT<dd>, const Store<dd>::C*);
+template void launch_passC_v<dd, dd, 1, 0>(cudaStream_t, int, Bufs<dd, dd>, PassArgs, PassK<dd, dd>, const Store<dd>::C*);
 }  // namespace laps

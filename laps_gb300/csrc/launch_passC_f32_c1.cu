@@ -1,0 +1,5 @@
+// Pass C launcher (float transforms, dd state, compressible, CFL 1).
+#include "launch_defs.cuh"
+namespace laps {
+template void launch_passC_v<float, dd, 0, 1>(cudaStream_t, int, Bufs<float, dd>, PassArgs, PassK<float, dd>, const Store<float>::C*);
+}  // namespace laps

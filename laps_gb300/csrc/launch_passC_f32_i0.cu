@@ -1,0 +1,5 @@
+// Pass C launcher (float transforms, dd state, incompressible, CFL 0).
+#include "launch_defs.cuh"
+namespace laps {
+template void launch_passC_v<float, dd, 1, 0>(cudaStream_t, int, Bufs<float, dd>, PassArgs, PassK<float, dd>, const Store<float>::C*);
+}  // namespace laps

@@ -1,5 +1,5 @@
-// Pass C launcher (double, incompressible, CFL 0).
+// Pass C launcher (double transforms, double state, incompressible, CFL 0).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passC_v<double, 1, 0>(cudaStream_t, int, Bufs<double>, PassArgs, PT<double>, const Store<double>::C*);
+template void launch_passC_v<double, double, 1, 0>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*);
 }  // namespace laps

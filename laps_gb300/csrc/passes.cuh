@@ -19,6 +19,8 @@ struct PassArgs {
   int mass_from_state;  // compressible, Nyquist modes zeroed by the dealiasing: the mass
                         // flux rho u is the state's momentum, so -i k.(rho u)^ is taken from U
                         // in pass E and passes C, D skip fluxes 1..3
+  int e_first;     // pass E: variable of blockIdx.z = 0 (the continuity update runs in a launch
+                   // of its own before the momentum is overwritten)
   StepState* st;
 };
 
@@ -50,8 +52,10 @@ __constant__ ATab c_atab[2][12] = {
     {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {7, 0}, {5, -1}, {4, 1}, {0, 0}, {0, 0}},
     {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {5, -1}, {4, 1}, {1, 1}, {2, 1}, {3, 1}}};
 
-template <class T, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
+template <class T, class TS, int NZ>
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;
   using C = typename Store<T>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -66,13 +70,13 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T> b, PassAr
   int ky = ok ? g.ky_of(r) : 0;
   long long col = (long long)ky * g.kxp + kx;  // + z * ny * kxp
   long long zs = (long long)g.ny * g.kxp;
-  const C* in = b.U + e.src * g.fsc + col;
+  const typename Store<TS>::C* in = b.U + e.src * g.fsc + col;
 #pragma unroll 4
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.kz_in(kz)) {
-      v = Store<T>::ldg(in + kz * zs);
+      v = cvtc<T>(Store<TS>::ldg(in + kz * zs));
       if (e.mult < 0) v = -mul_i(v, K.kzd[kz]);
       else if (e.mult > 0) v = mul_i(v, K.kzd[kz]);
     }
@@ -118,8 +122,10 @@ __device__ __forceinline__ cx<T> bterm(cx<T> v, int f, T ax, T ay) {
   }
 }
 
-template <class T, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twy) {
+template <class T, class TS, int NY>
+__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
   using CL = Col<T, NY>;
   using C = typename Store<T>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -129,7 +135,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassAr
   const int f = blockIdx.z;
   const int vt = a.P.variant == LAPS_VARIANT_3DI ? 2 : (a.P.two_d ? 1 : 0);
   const BTab e = c_btab[vt][f];
-  const C* src = a.P.two_d ? b.U : b.W1;
+  const bool from_state = a.P.two_d;
   int kx = blockIdx.x * TX + x.c;
   int z = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && z < g.nz;
@@ -141,11 +147,14 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T> b, PassAr
     int ky = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.ky_in(ky)) {
-      const C* w = src + col + (long long)ky * g.kxp;
+      const long long off = col + (long long)ky * g.kxp;
+      auto ld = [&](int f) {
+        return from_state ? cvtc<T>(Store<TS>::ldg(b.U + off + f * g.fsc)) : Store<T>::ldg(b.W1 + off + f * g.fsc);
+      };
       T ax = pc.zero, ay = pc.zero, az;
       if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
-      v = bterm(Store<T>::ldg(w + e.in0 * g.fsc), e.f0, ax, ay);
-      if (e.in1 >= 0) v = v + bterm(Store<T>::ldg(w + e.in1 * g.fsc), e.f1, ax, ay);
+      v = bterm(ld(e.in0), e.f0, ax, ay);
+      if (e.in1 >= 0) v = v + bterm(ld(e.in1), e.f1, ax, ay);
     }
     Store<T>::stc(x.at(0, m), v);
   }
@@ -341,8 +350,9 @@ template <int NX> struct PassCCfg {
   static constexpr int SMEM = ROWS * NF * LC * 16;
 };
 
-template <class T, int NX, int CFL, int INCOMP>
-__global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, PassArgs a, PT<T> pc, const typename Store<T>::C* __restrict__ twx) {
+template <class T, class TS, int NX, int CFL, int INCOMP>
+__global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twx) {
+  const PT<T>& pc = kk.pc;
   using CF = PassCCfg<NX>;
   using C = typename Store<T>::C;
   using SR = typename Store<T>::R;
@@ -375,9 +385,9 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
     fft_lines<T, CF::H, +1, 1, 0>(z, 0, lt, act, twx, 2);
   }
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
-  T tmin = Real<T>::inf();
+  TS tmin = Real<TS>::inf();
   bool nan_seen = false;
-  const T rfac = Real<T>::from_d(a.st->radius / a.P.R0);
+  const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
   const T inv_tau = Real<T>::from_d(a.st->inv_tau);
   const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
 #pragma unroll 1
@@ -389,15 +399,19 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T> b, P
 #pragma unroll
     for (int f = 0; f < NQ; f++) q[f] = f < nin ? Store<T>::ld(base + 2 * f * CF::LC) : pc.zero;
     using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
-    if (CFL) {
-      T d = PH::cfl(q, pc, a.P, rfac);
-      if (Real<T>::isnan_(d)) nan_seen = true;
-      else tmin = Real<T>::min_(tmin, d);
+    using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
+    if (CFL) {  // in the state type: FP64-equivalent even when the transforms run in FP32
+      TS qs[NQ];
+#pragma unroll
+      for (int f = 0; f < NQ; f++) qs[f] = Cvt<TS, T>::r(q[f]);
+      TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
+      if (Real<TS>::isnan_(d)) nan_seen = true;
+      else tmin = Real<TS>::min_(tmin, d);
     }
     if (nfl > 0) PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   if (CFL) {
-    double dmin = Real<T>::to_d(tmin);
+    double dmin = Real<TS>::to_d(tmin);
     for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmin;
     if (__any_sync(0xffffffffu, nan_seen) && (threadIdx.x & 31) == 0) atomicOr(&a.st->status, LAPS_STATUS_NAN);
@@ -453,8 +467,10 @@ __constant__ DGroup c_dgroups[2][8] = {
     {{{0, -1, -1}, DG_COPY, 0}, {{1, -1, -1}, DG_COPY, 1}, {{2, -1, -1}, DG_COPY, 2}, {{3, 4, -1}, DG_EXY, 3},
      {{5, -1, -1}, DG_EZ, 6}}};
 
-template <class T, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twy) {
+template <class T, class TS, int NY>
+__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
   using CL = Col<T, NY>;
   using C = typename Store<T>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -563,7 +579,7 @@ struct RkCtx {
     if (mom && P->visc && P->visc_exp) fnl = fnl - u * (pc->nu * k2);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc->eta * k2);
     cx<T> un = fnl * cc + u;
-    if (stage > 0) un = (fnl * cc + Store<T>::ldg(R) * ddc) + u;
+    if (stage > 0) un = (fnl * cc + Store<T>::ldc(R) * ddc) + u;  // coherent: R is rewritten below
     if (store_rk) Store<T>::stc(R, fnl);
     if (mom && P->visc && !P->visc_exp) {
       T d = ts * k2 * pc->nu + pc->one;
@@ -600,15 +616,17 @@ __device__ __forceinline__ RkCtx<T> rk_ctx(const PassArgs& a, const PT<T>& pc, c
 // Compressible: forward z-FFT with the kz parts of the right-hand side, then the tail and
 // the time advance of variable v = blockIdx.z.  Tile: kx0..kx0+7, one kept ky row; reads all
 // z of W2, writes kept kz of U (and R).
-template <class T, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
+template <class T, class TS, int NZ>
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;
   using C = typename Store<T>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if (a.st->halt) return;
   ColCtx<T, NZ, 2> x(reinterpret_cast<C*>(smem_raw));
   const Geo& g = a.g;
-  const int v = blockIdx.z;
+  const int v = blockIdx.z + a.e_first;
   int kx = blockIdx.x * TX + x.c;
   int r = blockIdx.y * CL::NTILE + x.tl;
   bool ok = kx < g.kx_keep && r < g.nky();
@@ -633,33 +651,34 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
     fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
   }
   if (!ok) return;
-  const RkCtx<T> rk = rk_ctx(a, pc, K);
+  using CS = typename Store<TS>::C;
+  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
   const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
-  C* U = b.U + v * g.fsc + col;
-  C* R = b.R + v * g.fsc + col;
+  CS* U = b.U + v * g.fsc + col;
+  CS* R = b.R + v * g.fsc + col;
 #pragma unroll 2
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     if (!g.kz_in(kz)) continue;
-    cx<T> fnl;
+    const long long idx = kz * zs;
+    cx<TS> fnl;
     if (nin == 0) {  // continuity: -i k . (rho u)^ from the momentum spectrum (mhdrhs.f90:206-209)
-      T ax, ay, az;
-      kfac(K, a.P, pc, rk.rr, kx, ky, kz, ax, ay, az);
-      const long long id = kz * zs;
-      fnl = -((mul_i(Store<T>::ldg(b.U + 1 * g.fsc + col + id), ax) + mul_i(Store<T>::ldg(b.U + 2 * g.fsc + col + id), ay)) +
-              mul_i(Store<T>::ldg(b.U + 3 * g.fsc + col + id), az));
+      TS ax, ay, az;
+      kfac(kk.KS, a.P, kk.ps, rk.rr, kx, ky, kz, ax, ay, az);
+      fnl = -((mul_i(Store<TS>::ldc(b.U + 1 * g.fsc + col + idx), ax) + mul_i(Store<TS>::ldc(b.U + 2 * g.fsc + col + idx), ay)) +
+              mul_i(Store<TS>::ldc(b.U + 3 * g.fsc + col + idx), az));
     } else {
-      fnl = Store<T>::ldc(x.at(0, m));
-      fnl = {Real<T>::mul_pow2(fnl.re, sexp), Real<T>::mul_pow2(fnl.im, sexp)};
+      cx<T> f = Store<T>::ldc(x.at(0, m));
+      f = {Real<T>::mul_pow2(f.re, sexp), Real<T>::mul_pow2(f.im, sexp)};
+      if (nin > 1) {
+        cx<T> w = Store<T>::ldc(x.at(1, m));
+        w = mul_i(cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)}, K.kzd[kz]);
+        f = v == 4 ? f + w : f - w;
+      }
+      fnl = cvtc<TS>(f);
     }
-    if (nin > 1) {
-      cx<T> w = Store<T>::ldc(x.at(1, m));
-      w = mul_i(cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)}, K.kzd[kz]);
-      fnl = v == 4 ? fnl + w : fnl - w;
-    }
-    long long idx = kz * zs;
-    T k2 = need_k2 ? rk.k2(kx, ky, kz) : pc.zero;
-    rk.update(v, fnl, Store<T>::ldg(U + idx), U + idx, R + idx, k2, kx, ky, kz);
+    TS k2 = need_k2 ? rk.k2(kx, ky, kz) : kk.ps.zero;
+    rk.update(v, fnl, Store<TS>::ldc(U + idx), U + idx, R + idx, k2, kx, ky, kz);
   }
 }
 
@@ -667,8 +686,10 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T> b, PassAr
 // transforms the pressure flux and updates rho, rho u and p:
 //   k.fp = (i k . fp_hat)/k^2, p_hat = -k.fp, fnl(rho u) = fp_hat + k.fp (i k)  (0 where k^2 < 1e-10)
 // groups 1..3 advance Bx, By, Bz from the electric field as in the compressible pass.
-template <class T, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T> b, PassArgs a, PT<T> pc, KTab<T> K, const typename Store<T>::C* __restrict__ twz) {
+template <class T, class TS, int NZ>
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;
   using C = typename Store<T>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -698,8 +719,9 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T> b, Pass
     fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
   }
   if (!ok) return;
-  const RkCtx<T> rk = rk_ctx(a, pc, K);
-  const T rr = rk.rr;
+  using CS = typename Store<TS>::C;
+  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
+  const T rr = Real<T>::from_d(a.st->r_ratio);
 #pragma unroll 1
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
@@ -709,34 +731,36 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T> b, Pass
       cx<T> w = Store<T>::ldc(x.at(bi, m));
       return cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)};
     };
-    T k2 = rk.k2(kx, ky, kz);
+    TS k2 = rk.k2(kx, ky, kz);
     if (grp == 0) {
       T ax, ay, az;
       kfac(K, a.P, pc, rr, kx, ky, kz, ax, ay, az);
+      const T k2t = Cvt<T, TS>::r(k2);
       cx<T> f0 = val(0), f1 = val(1), f2 = val(2);
-      const bool small = Real<T>::lead(k2) < 1e-10f;
+      const bool small = Real<T>::lead(k2t) < 1e-10f;
       cx<T> kdot = cx_zero<T>();
       if (!small) {
-        cx<T> s = (mul_i(f0, ax) + mul_i(f1, ay)) + mul_i(f2, az);
-        kdot = {s.re / k2, s.im / k2};
+        cx<T> sm = (mul_i(f0, ax) + mul_i(f1, ay)) + mul_i(f2, az);
+        kdot = {sm.re / k2t, sm.im / k2t};
       }
       const cx<T> fm[3] = {small ? cx_zero<T>() : f0 + mul_i(kdot, ax), small ? cx_zero<T>() : f1 + mul_i(kdot, ay),
                            small ? cx_zero<T>() : f2 + mul_i(kdot, az)};
       for (int v = 0; v < 4; v++) {
-        C* U = b.U + v * g.fsc + col + idx;
-        rk.update(v, v == 0 ? cx_zero<T>() : fm[v - 1], Store<T>::ldg(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
+        CS* U = b.U + v * g.fsc + col + idx;
+        rk.update(v, v == 0 ? cx_zero<TS>() : cvtc<TS>(fm[v - 1]), Store<TS>::ldc(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky,
+                  kz);
       }
-      C* U = b.U + 7 * g.fsc + col + idx;  // the new pressure replaces slot 8 before the update
-      rk.update(7, cx_zero<T>(), -kdot, U, b.R + 7 * g.fsc + col + idx, k2, kx, ky, kz);
+      CS* U = b.U + 7 * g.fsc + col + idx;  // the new pressure replaces slot 8 before the update
+      rk.update(7, cx_zero<TS>(), cvtc<TS>(-kdot), U, b.R + 7 * g.fsc + col + idx, k2, kx, ky, kz);
     } else {
       const int v = 3 + grp;
-      cx<T> fnl = val(0);
+      cx<T> f = val(0);
       if (nin > 1) {
         cx<T> w = mul_i(val(1), K.kzd[kz]);
-        fnl = v == 4 ? fnl + w : fnl - w;
+        f = v == 4 ? f + w : f - w;
       }
-      C* U = b.U + v * g.fsc + col + idx;
-      rk.update(v, fnl, Store<T>::ldg(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
+      CS* U = b.U + v * g.fsc + col + idx;
+      rk.update(v, cvtc<TS>(f), Store<TS>::ldc(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
     }
   }
 }
