@@ -6,10 +6,16 @@ Ur0/R0 = 0.01, eta = nu = 5e-4, 2/3 mask, cfl 0.4, random-phase 1 <= |k| <= 8 sp
 rms 0.5, seed 1), seeded synthetic initial condition.  A "step" is one full time step
 (CFL, three RK stages, radius update) of the whole grid.
 
-Our arm (default): the float-float engine through the C-ABI.  `value` is device-timed with
-CUDA events on the engine's stream, state resident in HBM; `e2e` is the same metric through
-the C-ABI with host buffers (pinned upload of the primitive initial state, one laps_step call
-per step returning time/dt/status to the host, download of the final state).
+Our arm (default --precision fp32): the FP32-transform engine (FP32 transforms and nonlinear
+products; state, RK accumulation, CFL and diagnostics in float-float) through the C-ABI,
+timed beside the plain paths on the same workload (`plain`: the float-float engine, which
+matches FP64 to 1e-10, and the native FP64 engine) and with its error against the FP64
+engine stated (`error_vs_fp64`: per-field relative L2, invariants and the E(k) shell spectra
+after --err-steps steps).  `value` is device-timed with CUDA events on the engine's stream,
+state resident in HBM; `e2e` is the same metric through the C-ABI with host buffers (pinned
+upload of the primitive initial state, one laps_step call per step returning time/dt/status
+to the host, download of the final state).  --precision dd / fp64 / fp32_f64 time those
+modes as the headline instead.
 
 --impl reference: the reference's CPU algorithm (the oracle restatement, pocketfft with all
 host threads) timed on a bounded sample of the same workload.
@@ -176,12 +182,13 @@ def cpu_sample(steps, warmup, n=None):
 
 
 def fp32_error(p, prim, steps):
-    """Per-field relative L2 error and invariant error of an FP32-transform run against the FP64
-    engine after `steps` steps of the same workload (the FP64 engine matches the oracle to
-    1e-10 at these step counts)."""
+    """Error of an FP32-transform run against the FP64 engine after `steps` steps of the same
+    workload (the FP64 engine matches the oracle to 1e-10): per-field relative L2, the
+    invariants, the time, and the shell spectra E_u(k), E_b(k) over 1 <= k <= k_max / 2
+    (k_max = n/3, the 2/3 sphere)."""
     from laps_gb300 import ffi
 
-    out = {}
+    nshell = max(p.nx, p.ny, p.nz) // 3 + 1
     runs = {}
     for name, mode in (("test", p.precision), ("fp64", ffi.PREC_FP64)):
         q = ffi.laps_params.from_buffer_copy(p)
@@ -192,16 +199,39 @@ def fp32_error(p, prim, steps):
         t, dt, st = r.step(steps)
         uu, _ = r.download_state()
         d = r.diagnostics()
-        runs[name] = (uu, np.array([d.e_kin, d.e_mag, d.h_cross, d.h_mag]), t)
+        eu, eb = r.spectrum(nshell)
+        runs[name] = (uu, np.array([d.e_kin, d.e_mag, d.h_cross, d.h_mag]), t, eu, eb)
         r.close()
     a, b = runs["test"], runs["fp64"]
     rel = [float(np.linalg.norm(a[0][f] - b[0][f]) / max(np.linalg.norm(b[0][f]), 1e-300)) for f in range(8)]
-    out["steps"] = steps
-    out["field_rel_l2"] = rel
-    out["max_field_rel_l2"] = max(rel)
-    out["invariants_rel"] = [float(v) for v in np.abs(a[1] - b[1]) / np.maximum(np.abs(b[1]), 1e-300)]
-    out["time_rel"] = abs(a[2] - b[2]) / b[2]
+    half = slice(1, (nshell - 1) // 2 + 1)
+    out = {"steps": steps, "field_rel_l2": rel, "max_field_rel_l2": max(rel),
+           "invariants_rel": [float(v) for v in np.abs(a[1] - b[1]) / np.maximum(np.abs(b[1]), 1e-300)],
+           "time_rel": abs(a[2] - b[2]) / b[2],
+           "spectrum_shells": f"1..{half.stop - 1}"}
+    for key, i in (("u", 3), ("b", 4)):
+        ea, eb = a[i][half], b[i][half]
+        relk = np.abs(ea - eb) / np.maximum(eb, 1e-300)
+        live = eb >= 1e-6 * eb.max()  # shells holding at least 1e-6 of the largest
+        out[f"spectrum_{key}_rel_by_shell"] = [float(f"{v:.3g}") for v in relk]
+        out[f"spectrum_{key}_max_rel_live_shells"] = float(relk[live].max())
+        out[f"spectrum_{key}_max_abs_over_total"] = float(np.abs(ea - eb).max() / eb.sum())
     return out
+
+
+def device_timed(p, prim, steps, warmup):
+    """Steps of one context timed with CUDA events around every pass (state resident in HBM):
+    (per-pass ms, total ms, status, info)."""
+    from laps_gb300 import ffi
+
+    g = ffi.Laps(p)
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    g.step(warmup)
+    info = g.info()
+    pass_ms, total_ms, status = g.step_profiled(steps)
+    g.close()
+    return pass_ms, total_ms, status, info
 
 
 def run_reference(args):
@@ -288,6 +318,20 @@ def run_ours(args):
     h2d = host_in.nbytes / args.steps + 16
     d2h = (host_out.nbytes + host_prim.nbytes) / args.steps + 128
     e2e_ctx.close()
+    g.close()
+    # ---- the plain paths on the same workload (FP64-parity float-float, native FP64)
+    plain = {}
+    if not args.no_plain and rank == 0 and ws == 1:
+        for mode in ("dd", "fp64"):
+            if mode == args.precision:
+                continue
+            q = ffi.laps_params.from_buffer_copy(p)
+            q.precision = PRECISIONS[mode][0]
+            pm, tm, st_p, _ = device_timed(q, prim, args.steps, max(args.warmup, 3))
+            v = npts * args.steps / (tm * 1e-3)
+            plain[mode] = {"value": v, "ms_per_step": tm / args.steps, "status": st_p,
+                           "dtype": PRECISIONS[mode][1],
+                           "pass_ms_per_step": {PASS_NAMES[i]: pm[i] / args.steps for i in range(6)}}
     # ---- roofline of the dominant pass
     nky, nkz = info.ky_keep, info.kz_keep
     eS, eT = PRECISIONS[args.precision][2:4]
@@ -324,6 +368,9 @@ def run_ours(args):
                 "pinned": pinned},
         "clocks": clk.summary(),
     }
+    if plain:
+        line["plain"] = plain
+        line["vs_plain"] = {k: value / v["value"] for k, v in plain.items()}
     if args.precision.startswith("fp32") and not SHAPE and not args.no_err:
         line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -331,7 +378,6 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    g.close()
     if ws > 1:
         import torch.distributed as dist
 
@@ -346,7 +392,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="dd", choices=list(PRECISIONS))
+    ap.add_argument("--precision", default="fp32", choices=list(PRECISIONS))
+    ap.add_argument("--no-plain", action="store_true", dest="no_plain",
+                    help="skip timing the plain float-float and FP64 paths beside the headline mode")
     ap.add_argument("--err-steps", type=int, default=10, dest="err_steps",
                     help="steps of the FP32-vs-FP64 error check of the fp32 modes")
     ap.add_argument("--no-err", action="store_true", dest="no_err")

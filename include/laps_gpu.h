@@ -176,6 +176,14 @@ int laps_upload_spectral(laps_ctx* ctx, const double* uf);
  * kinetic/magnetic energy, cross- and magnetic helicity of the current state. */
 int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
 
+/* Shell energy spectra of the current state: e_u[s] = 1/2 sum |u_hat|^2 (velocity
+ * u = rho u / rho) and e_b[s] = 1/2 sum |B_hat|^2 over the modes with round(|k|/dk) = s,
+ * s < nshell (1..2048), |k| from the unscaled grid wave numbers, dk = 2 pi / max(L); the
+ * shells sum to <u^2>/2 and <B^2>/2.  Replaces the reference's post-processing of the
+ * output files (data_process/3D_Python/fourier_analysis.py:150-200), which has no shell
+ * binning of its own.  Either array may be NULL. */
+int laps_spectrum(laps_ctx* ctx, int nshell, double* e_u, double* e_b);
+
 /* Forward transform of nfields real FP64 fields that allocates no device memory, for hosts
  * that cannot call cudaMalloc (their device memory comes from their own pool or framework,
  * or allocation is not allowed after start-up).  No counterpart in the reference: it is the

@@ -152,6 +152,10 @@ int laps_diagnostics(laps_ctx* c, laps_diag* d) {
   if (!d) return fail(c, LAPS_EINVAL, "null diag");
   return guarded(c, [&] { c->e->diagnostics(d); });
 }
+int laps_spectrum(laps_ctx* c, int nshell, double* e_u, double* e_b) {
+  if (!e_u && !e_b) return fail(c, LAPS_EINVAL, "null spectrum arrays");
+  return guarded(c, [&] { c->e->spectrum(nshell, e_u, e_b); });
+}
 int laps_wait(laps_ctx* c, int timeout_ms) { return guarded(c, [&] { c->e->wait(timeout_ms); }); }
 int laps_get_time(laps_ctx* c, double* t, double* dt) { return guarded(c, [&] { c->e->get_time(t, dt); }); }
 int laps_get_info(laps_ctx* c, laps_info* i) {

@@ -156,4 +156,80 @@ __global__ void __launch_bounds__(256) k_max_abs(const typename Store<T>::R* __r
   }
 }
 
+// u_i = (rho u_i) / rho in place on the real fields 1..3 (field 0 = rho), field pitch n
+template <class T>
+__global__ void __launch_bounds__(256) k_velocity(typename Store<T>::R* __restrict__ u, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T r = Store<T>::ld(u + i);
+#pragma unroll
+    for (int c = 1; c <= 3; c++) Store<T>::st(u + c * n + i, Store<T>::ld(u + c * n + i) / r);
+  }
+}
+
+// Shell spectra of two 3-component half spectra (pitch `pitch`): 1/2 |u_hat|^2 and
+// 1/2 |B_hat|^2 summed over the modes with round(|k| inv_dk) = s < nshell, |k| from the
+// unscaled wave numbers, modes 0 < kx < nx/2 counted twice.  Deterministic: a warp adds the
+// lanes that share a shell in lane order (__match_any_sync), keeps its own shell array in
+// shared memory, and the block adds its 4 warp arrays in order; the host adds the blocks.
+constexpr int SPEC_WARPS = 4;
+template <class T>
+__global__ void __launch_bounds__(SPEC_WARPS * 32) k_shell_spectrum(const typename Store<T>::C* __restrict__ uh,
+                                                                    const typename Store<T>::C* __restrict__ bh, long long pitch,
+                                                                    Geo g, const double* __restrict__ wx, const double* __restrict__ wy,
+                                                                    const double* __restrict__ wz, double inv_dk, int nshell,
+                                                                    double* __restrict__ part) {
+  extern __shared__ double sh[];  // [SPEC_WARPS][2][nshell]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < SPEC_WARPS * 2 * nshell; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  double* mine = sh + warp * 2 * nshell;
+  const long long tot = (long long)g.nz * g.ny * g.nh;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x + warp * 32; base < tot; base += stride) {
+    const long long i = base + lane;
+    int key = -1;
+    double eu = 0.0, eb = 0.0;
+    if (i < tot) {
+      const int kx = (int)(i % g.nh);
+      const long long r = i / g.nh;
+      const int ky = (int)(r % g.ny), kz = (int)(r / g.ny);
+      const double kk = sqrt(wx[kx] * wx[kx] + wy[ky] * wy[ky] + wz[kz] * wz[kz]);
+      const int s = (int)floor(kk * inv_dk + 0.5);
+      if (s < nshell) {
+        key = s;
+        const long long idx = (long long)kz * g.ny * g.kxp + (long long)ky * g.kxp + kx;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          cx<T> a = Store<T>::ldc(uh + c * pitch + idx), b = Store<T>::ldc(bh + c * pitch + idx);
+          double ar = Real<T>::to_d(a.re), ai = Real<T>::to_d(a.im), br = Real<T>::to_d(b.re), bi = Real<T>::to_d(b.im);
+          eu += ar * ar + ai * ai;
+          eb += br * br + bi * bi;
+        }
+        const double w = (kx == 0 || 2 * kx == g.nx) ? 0.5 : 1.0;
+        eu *= w;
+        eb *= w;
+      }
+    }
+    const unsigned m = __match_any_sync(0xffffffffu, key);
+    double su = 0.0, sb = 0.0;
+    for (int l = 0; l < 32; l++) {
+      const double xu = __shfl_sync(0xffffffffu, eu, l), xb = __shfl_sync(0xffffffffu, eb, l);
+      if ((m >> l) & 1u) {
+        su += xu;
+        sb += xb;
+      }
+    }
+    if (key >= 0 && lane == __ffs(m) - 1) {
+      mine[key] += su;
+      mine[nshell + key] += sb;
+    }
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < 2 * nshell; s += blockDim.x) {
+    double acc = 0.0;
+    for (int w = 0; w < SPEC_WARPS; w++) acc += sh[w * 2 * nshell + s];
+    part[(size_t)blockIdx.x * 2 * nshell + s] = acc;
+  }
+}
+
 }  // namespace laps

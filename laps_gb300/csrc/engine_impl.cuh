@@ -55,6 +55,7 @@ class EngineBase {
   virtual void download_spectral(double* uf) = 0;
   virtual void upload_spectral(const double* uf) = 0;
   virtual void diagnostics(laps_diag* d) = 0;
+  virtual void spectrum(int nshell, double* eu, double* eb) = 0;
   virtual void wait(int timeout_ms) = 0;
   virtual void get_time(double* t, double* dt) = 0;
   virtual void info(laps_info* i) = 0;
@@ -584,6 +585,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
     wait(tmo());
   }
   void diagnostics(laps_diag* d) override;
+  void spectrum(int nshell, double* eu, double* eb) override;
+  double* d_spec = nullptr;  // per-block shell partials of spectrum()
+  size_t spec_cap = 0;
   void get_time(double* t, double* dt) override {
     read_state();
     if (t) *t = h_st->time;
@@ -603,6 +607,45 @@ template <class T, class TS = T> class Engine : public EngineBase {
 };
 
 // ---------------------------------------------------------------------------- diagnostics
+template <class T, class TS> void Engine<T, TS>::spectrum(int nshell, double* eu, double* eb) {
+  if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+  if (nshell < 1 || nshell > 2048) throw Error{LAPS_EINVAL, "nshell must be in [1, 2048]"};
+  const Geo& g = gfull;
+  read_state();
+  // velocity u = (rho u) / rho in real space, then its half spectrum in W2 fields 3..5
+  inverse3d(B.U, 4);
+  k_velocity<TS><<<1024, 256, 0, stream>>>((SRS*)B.W1, g.fsr);
+  LAPS_CK(cudaGetLastError());
+  CS* uh = W2s() + 3 * g.fsc;
+  forward3d((const SRS*)B.W1 + g.fsr, uh, 3);
+  const int nb = 304;
+  const size_t need = (size_t)nb * 2 * nshell;
+  if (spec_cap < need) {
+    d_spec = dalloc<double>(need);
+    spec_cap = need;
+  }
+  double lmax = std::fmax(p.Lx, p.Ly);
+  if (p.nz > 1) lmax = std::fmax(lmax, p.Lz);
+  const double dk = 2.0 * 3.141592653589793 / lmax;
+  const int smem = SPEC_WARPS * 2 * nshell * (int)sizeof(double);
+  set_smem(k_shell_spectrum<TS>, smem);
+  k_shell_spectrum<TS><<<nb, SPEC_WARPS * 32, smem, stream>>>(uh, B.U + 4 * g.fsc, g.fsc, g, d_wx, d_wy, d_wz, 1.0 / dk,
+                                                              nshell, d_spec);
+  LAPS_CK(cudaGetLastError());
+  std::vector<double> part(need);
+  LAPS_CK(cudaMemcpyAsync(part.data(), d_spec, need * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  wait(tmo());
+  for (int s = 0; s < nshell; s++) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nb; k++) {
+      a += part[(size_t)k * 2 * nshell + s];
+      b += part[(size_t)k * 2 * nshell + nshell + s];
+    }
+    if (eu) eu[s] = a;
+    if (eb) eb[s] = b;
+  }
+}
+
 template <class T, class TS> void Engine<T, TS>::diagnostics(laps_diag* d) {
   if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
   const Geo& g = gfull;

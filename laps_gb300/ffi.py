@@ -97,6 +97,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_download_spectral": (C.c_int, [vp, dp]),
         "laps_upload_spectral": (C.c_int, [vp, dp]),
         "laps_diagnostics": (C.c_int, [vp, P(laps_diag)]),
+        "laps_spectrum": (C.c_int, [vp, C.c_int, dp, dp]),
         "laps_wait": (C.c_int, [vp, C.c_int]),
         "laps_get_time": (C.c_int, [vp, dp, dp]),
         "laps_get_info": (C.c_int, [vp, P(laps_info)]),
@@ -212,6 +213,13 @@ class Laps:
         d = laps_diag()
         self._ck(self.lib.laps_diagnostics(self.h, C.byref(d)))
         return d
+
+    def spectrum(self, nshell: int):
+        """Shell spectra (e_u, e_b) of the current state, nshell shells of width 2 pi / max(L)."""
+        eu = np.zeros(nshell)
+        eb = np.zeros(nshell)
+        self._ck(self.lib.laps_spectrum(self.h, int(nshell), _dptr(eu), _dptr(eb)))
+        return eu, eb
 
     def time(self):
         t, d = C.c_double(), C.c_double()

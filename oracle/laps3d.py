@@ -525,6 +525,37 @@ def magnetic_helicity(bf, kx, ky, kz, nx):
     return float(np.sum(dens * w[None, None, :]))
 
 
+def shell_spectra(uu: np.ndarray, Lx: float, Ly: float, Lz: float, nshell: int):
+    """Shell energy spectra E_u(k) = 1/2 sum |u_hat|^2 and E_b(k) = 1/2 sum |B_hat|^2.
+
+    u = (rho u)/rho from the conserved real fields ``uu[0:4]``, B = ``uu[4:7]``; hats are the
+    reference's forward transform (divided by n per axis, ``fftw.f90:42-71``), so the shells
+    sum to <u^2>/2 and <B^2>/2.  Shell s holds the modes with round(|k|/dk) = s, |k| from the
+    grid's unscaled wave numbers (``mhdinit.f90:88-115``) and dk = 2 pi / max(L) over the
+    axes with more than one point; modes beyond the last shell are dropped.  The reference
+    post-processes |B_hat|^2 the same way with numpy's fftn
+    (``data_process/3D_Python/fourier_analysis.py:150-200``); the shell binning is this
+    solver's own.  A half spectrum counts modes 0 < kx < nx/2 twice.
+    """
+    nz, ny, nx = uu.shape[-3:]
+    u = uu[1:4] / uu[0]
+    uh = forward_3d(u)
+    bh = forward_3d(uu[4:7])
+    kx = wave_numbers(nx, Lx)[: nx // 2 + 1]
+    ky = wave_numbers(ny, Ly)
+    kz = wave_numbers(nz, Lz) if nz > 1 else np.zeros(1)
+    Ls = [L for L, n in ((Lx, nx), (Ly, ny), (Lz, nz)) if n > 1]
+    dk = 2 * PI / max(Ls)
+    kk = np.sqrt(kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2)
+    shell = np.floor(kk / dk + 0.5).astype(np.int64)
+    w = np.where((np.arange(nx // 2 + 1) == 0) | (2 * np.arange(nx // 2 + 1) == nx), 1.0, 2.0)[None, None, :]
+    eu = 0.5 * w * np.sum(np.abs(uh) ** 2, axis=0)
+    eb = 0.5 * w * np.sum(np.abs(bh) ** 2, axis=0)
+    keep = shell < nshell
+    return (np.bincount(shell[keep], eu[keep], minlength=nshell)[:nshell],
+            np.bincount(shell[keep], eb[keep], minlength=nshell)[:nshell])
+
+
 def params_from(n, kw) -> Params3D:
     """Params3D for an n^3 (or (nx, ny, nz)) grid from C-ABI-style keyword values."""
     nx, ny, nz = (n, n, n) if np.isscalar(n) else n

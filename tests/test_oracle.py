@@ -153,3 +153,25 @@ def test_golden_fixture(path):
     for f in range(8):
         assert np.linalg.norm(o.uu[f] - g["uu"][f]) <= 1e-12 * max(np.linalg.norm(g["uu"][f]), 1e-300)
     assert np.allclose(o.invariants(), g["inv"], rtol=1e-11, atol=1e-15)
+
+
+def test_shell_spectra_parseval_and_single_mode():
+    """The shells of the oracle's spectrum sum to <u^2>/2 and <B^2>/2 (Parseval, half
+    spectrum weights), and a single Fourier mode lands in its own shell."""
+    from laps_gb300.ic import turbulence_ic
+    from oracle import laps3d
+
+    prim = turbulence_ic((16, 8, 4), seed=5)
+    o = laps3d.restart((16, 8, 4), {}, prim)
+    eu, eb = laps3d.shell_spectra(o.uu, 2 * np.pi, 2 * np.pi, 2 * np.pi, 32)
+    u = o.uu[1:4] / o.uu[0]
+    assert abs(eu.sum() - 0.5 * np.mean(np.sum(u ** 2, axis=0))) < 1e-14
+    assert abs(eb.sum() - 0.5 * np.mean(np.sum(o.uu[4:7] ** 2, axis=0))) < 1e-14
+    n = 16
+    x = np.arange(n) * 2 * np.pi / n
+    uu = np.zeros((8, n, n, n))
+    uu[0] = 1.0
+    uu[4] = np.cos(3 * x)[None, None, :]            # |k| = 3, energy 1/4
+    uu[5] = np.sin(4 * x)[None, :, None]            # |k| = 4, energy 1/4
+    _, eb = laps3d.shell_spectra(uu, 2 * np.pi, 2 * np.pi, 2 * np.pi, 8)
+    assert np.allclose(eb, [0, 0, 0, 0.25, 0.25, 0, 0, 0], atol=1e-15)
