@@ -136,10 +136,17 @@ __device__ __forceinline__ cx<T> twiddle(const typename Store<T>::C* __restrict_
 template <int JS> __device__ __forceinline__ int sm_idx(int j) { return JS == 1 ? j + (j >> 4) : j * JS; }
 template <int N> struct RowLen { static constexpr int V = N + N / 16; };  // padded length of a row line
 
+// Barrier of a stage: the whole block, or only the warp when every line's threads and shared
+// memory belong to one warp (WL: row lines of at most 32 threads, laid out consecutively).
+template <bool WL> __device__ __forceinline__ void stage_sync() {
+  if (WL) __syncwarp();
+  else __syncthreads();
+}
+
 // One Stockham stage of radix R after ns points have been combined (ns a power of two, 1
 // for the first stage: no twiddles), for every line of the tile.  Thread t of line l;
 // threads with active == false only join the two barriers.
-template <class T, int N, int DIR, int R, int JS, int LS>
+template <class T, int N, int DIR, int R, int JS, int LS, bool WL = false>
 __device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t, bool active, int ns, int lns,
                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
   using P = Plan<N>;
@@ -160,7 +167,7 @@ __device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t,
       }
     }
   }
-  __syncthreads();
+  stage_sync<WL>();
   if (active) {
 #pragma unroll
     for (int q = 0; q < NB; q++) {
@@ -172,29 +179,30 @@ __device__ __forceinline__ void fft_stage(typename Store<T>::C* s, int l, int t,
       for (int i = 0; i < R; i++) Store<T>::stc(line + sm_idx<JS>(base + i * ns), v[q][i]);
     }
   }
-  __syncthreads();
+  stage_sync<WL>();
 }
 
-// Full FFT of every line of the tile (unnormalised).  Every thread of the block calls it.
-// The radix-16 stages run in a rolled loop (one copy of their code); the last radix-2/4/8
-// stage follows.  tw: table of exp(-2 pi i j / (N*twstep)), j = 0..N*twstep-1.
-template <class T, int N, int DIR, int JS, int LS>
+// Full FFT of every line of the tile (unnormalised).  Every thread of the block (WL: of the
+// warp) calls it.  The radix-16 stages run in a rolled loop (one copy of their code); the last
+// radix-2/4/8 stage follows.  tw: table of exp(-2 pi i j / (N*twstep)), j = 0..N*twstep-1.
+template <class T, int N, int DIR, int JS, int LS, bool WL = false>
 __device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t, bool active,
                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
   using P = Plan<N>;
+  static_assert(!WL || (JS == 1 && P::TPL <= 32), "warp-local lines are rows of at most one warp");
   if constexpr (N == 1) {  // a length-1 transform is the identity (nz = 1)
-    __syncthreads();
+    stage_sync<WL>();
   } else if constexpr (N < 16) {
-    fft_stage<T, N, DIR, N, JS, LS>(s, l, t, active, 1, 0, tw, twstep);
+    fft_stage<T, N, DIR, N, JS, LS, WL>(s, l, t, active, 1, 0, tw, twstep);
   } else {
     int ns = 1, lns = 0;
 #pragma unroll 1
     for (int st = 0; st < P::NS16; st++) {
-      fft_stage<T, N, DIR, 16, JS, LS>(s, l, t, active, ns, lns, tw, twstep);
+      fft_stage<T, N, DIR, 16, JS, LS, WL>(s, l, t, active, ns, lns, tw, twstep);
       ns <<= 4;
       lns += 4;
     }
-    if constexpr (P::REST > 1) fft_stage<T, N, DIR, P::REST, JS, LS>(s, l, t, active, ns, lns, tw, twstep);
+    if constexpr (P::REST > 1) fft_stage<T, N, DIR, P::REST, JS, LS, WL>(s, l, t, active, ns, lns, tw, twstep);
   }
 }
 

@@ -129,7 +129,7 @@ template <class T, class TS, int INCOMP, int CFL>
 void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw) {
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
-    using CF = PassCCfg<NN>;                                                                                            \
+    using CF = PassCCfg<NN, (int)sizeof(typename Store<T>::C)>;                                                         \
     unsigned nb = (unsigned)((long long)a.g.ny * a.g.nz / CF::ROWS);                                                    \
     set_smem(k_passC<T, TS, NN, CFL, INCOMP>, CF::SMEM);                                                                \
     k_passC<T, TS, NN, CFL, INCOMP><<<nb, CF::THREADS, CF::SMEM, stream>>>(B, a, kk, tw);                               \

@@ -328,8 +328,6 @@ struct FluxI {
   }
 };
 
-// rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
-// (Hall) in one batch and their 38 outputs in two
 // pass C transform lists (flux slot numbers): compressible, compressible with the continuity
 // term from the state, incompressible; the expansion term 18 is last and dropped without it
 __constant__ int c_flist[3][16] = {{0, 1, 2, 3, 4, 5, 7, 8, 11, 12, 13, 14, 15, 16, 17, 18},
@@ -338,23 +336,34 @@ __constant__ int c_flist[3][16] = {{0, 1, 2, 3, 4, 5, 7, 8, 11, 12, 13, 14, 15, 
 // slots the physics has to store (all but 6, 9, 10; in the incompressible case all of 0..5)
 constexpr unsigned c_fused = 0x7FFFFu & ~((1u << 6) | (1u << 9) | (1u << 10));
 
-template <int NX> struct PassCCfg {
+// Rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
+// (Hall) in one batch; when two rows of 19 line slots do not fit in shared memory (1024-point
+// rows of 16-byte elements) a block takes one row and batches of 12 lines.
+template <int NX, int CB> struct PassCCfg {
   static constexpr int H = NX / 2;
   static constexpr int TPL = Plan<H>::TPL;
   static constexpr int MUL = TPL >= 4 ? 1 : 4 / TPL;
-  static constexpr int LB = 24 * MUL;       // lines per batch
-  static constexpr int THREADS = LB * TPL;
-  static constexpr int ROWS = 2 * MUL;
   static constexpr int NF = 19;             // line slots per row
   static constexpr int LC = RowLen<H>::V;   // padded complex per line
-  static constexpr int SMEM = ROWS * NF * LC * 16;
+  static constexpr bool ONE_ROW = 2 * MUL * NF * LC * CB > 200 * 1024;
+  static constexpr int LB = ONE_ROW ? 12 : 24 * MUL;  // lines per batch
+  static constexpr int THREADS = LB * TPL;
+  static constexpr int ROWS = ONE_ROW ? 1 : 2 * MUL;
+  static constexpr int SMEM = ROWS * NF * LC * CB;  // CB: bytes of one complex element
+  // resident blocks per SM the register budget is set for: at most 3 (FP32 lines) or 2,
+  // within the shared memory and the 2048 threads of an SM
+  static constexpr int OCC0 = CB == 8 ? 3 : 2;
+  static constexpr int OCC1 = (227 * 1024) / (SMEM + 1024) < OCC0 ? (227 * 1024) / (SMEM + 1024) : OCC0;
+  static constexpr int OCC2 = 2048 / THREADS < OCC1 ? 2048 / THREADS : OCC1;
+  static constexpr int OCC = OCC2 < 1 ? 1 : OCC2;
 };
 
 template <class T, class TS, int NX, int CFL, int INCOMP>
-__global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twx) {
+__global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)>::THREADS,
+                                  PassCCfg<NX, (int)sizeof(typename Store<T>::C)>::OCC) k_passC(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twx) {
   const PT<T>& pc = kk.pc;
-  using CF = PassCCfg<NX>;
   using C = typename Store<T>::C;
+  using CF = PassCCfg<NX, (int)sizeof(C)>;
   using SR = typename Store<T>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
@@ -381,9 +390,11 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T, TS> 
       int kk = g.kx_keep;
       c2r_pre<T, CF::H>(z, lt, [&](int k) { return k < kk ? Store<T>::ldg(xin + k) : cx_zero<T>(); }, twx);
     }
-    __syncthreads();
-    fft_lines<T, CF::H, +1, 1, 0>(z, 0, lt, act, twx, 2);
+    // a line and its threads stay within one warp until the physics reads across lines
+    __syncwarp();
+    fft_lines<T, CF::H, +1, 1, 0, true>(z, 0, lt, act, twx, 2);
   }
+  __syncthreads();
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
   TS tmin = Real<TS>::inf();
   bool nan_seen = false;
@@ -430,7 +441,7 @@ __global__ void __launch_bounds__(PassCCfg<NX>::THREADS, 2) k_passC(Bufs<T, TS> 
     bool act = L < CF::ROWS * nfl;
     int rr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
     C* z = sc + (rr * CF::NF + f) * CF::LC;
-    fft_lines<T, CF::H, -1, 1, 0>(z, 0, lt, act, twx, 2);
+    fft_lines<T, CF::H, -1, 1, 0, true>(z, 0, lt, act, twx, 2);
     if (act) {
       C* xo = b.W1 + f * g.fsc + (row0 + rr) * g.kxp;
       int kk = g.kx_keep;
