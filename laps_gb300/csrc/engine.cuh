@@ -82,6 +82,20 @@ template <class T> struct PT {
   T ebm[8];          // expansion damping factor of each variable
 };
 
+// the constants in FP32 (the CFL screen)
+template <class T> __device__ __forceinline__ PT<float> pt_float(const PT<T>& c) {
+  PT<float> f;
+  f.gamma = Cvt<float, T>::r(c.gamma); f.gm1 = Cvt<float, T>::r(c.gm1); f.cg = Cvt<float, T>::r(c.cg);
+  f.di = Cvt<float, T>::r(c.di); f.nu = Cvt<float, T>::r(c.nu); f.eta = Cvt<float, T>::r(c.eta);
+  f.cosc = Cvt<float, T>::r(c.cosc); f.sinc = Cvt<float, T>::r(c.sinc); f.inv_mindx = Cvt<float, T>::r(c.inv_mindx);
+  f.half = 0.5f; f.two = 2.f; f.one = 1.f; f.zero = 0.f; f.four = 4.f; f.is2 = Cvt<float, T>::r(c.is2);
+  f.dx = Cvt<float, T>::r(c.dx); f.dy = Cvt<float, T>::r(c.dy); f.dz = Cvt<float, T>::r(c.dz);
+  f.eta_dx = Cvt<float, T>::r(c.eta_dx); f.eta_dy = Cvt<float, T>::r(c.eta_dy);
+#pragma unroll
+  for (int v = 0; v < 8; v++) f.ebm[v] = Cvt<float, T>::r(c.ebm[v]);
+  return f;
+}
+
 // everything a pass needs in the compute type T and in the state type TS
 template <class T, class TS> struct PassK {
   PT<T> pc;

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(Col<T, N>::THREADS)
   long long base = (long long)blockIdx.z * fs + (long long)outer * ostride + col;
   C* s = sm + tl * N * TX;
   bool ok = col < ncol && outer < nouter;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < CL::EPT; m++) {
     int j = t + m * CL::TPL;
     cx<T> v = ok ? Store<T>::ldc(in + base + (long long)j * jstride) : cx_zero<T>();  // in may equal out

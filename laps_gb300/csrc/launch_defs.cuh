@@ -101,8 +101,7 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
     PassArgs a0 = a;                                                                                                    \
     a0.e_first = 0;                                                                                                     \
     if (a.mass_from_state) { /* continuity from the momentum first, then variables 1..7 */                             \
-      grid.z = 1;                                                                                                       \
-      k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw);                                   \
+      k_mass_rk<T, TS><<<4 * 152, 256, 0, stream>>>(B, a, kk);                                                          \
       a0.e_first = 1;                                                                                                   \
       grid.z = 7;                                                                                                       \
     }                                                                                                                   \

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T, TS> b, Pa
   long long col = (long long)ky * g.kxp + kx;  // + z * ny * kxp
   long long zs = (long long)g.ny * g.kxp;
   const typename Store<TS>::C* in = b.U + e.src * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     cx<T> v = cx_zero<T>();
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T, TS> b, Pa
   fft_lines<T, NZ, +1, TX, 1>(x.buf(0), x.c, x.t, true, twz, 1);
   if (!ok) return;
   C* out = b.W1 + f * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < CL::EPT; m++) Store<T>::stc(out + x.j(m) * zs, Store<T>::ldc(x.at(0, m)));
 }
 
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T, TS> b, Pa
   long long col = (long long)z * g.ny * g.kxp + kx;  // + y * kxp
   T rr = Real<T>::from_d(a.st->r_ratio);
   const bool kf = e.f0 > 1 || e.f0 < 0 || e.f1 > 1 || e.f1 < 0;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < CL::EPT; m++) {
     int ky = x.j(m);
     cx<T> v = cx_zero<T>();
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T, TS> b, Pa
   fft_lines<T, NY, +1, TX, 1>(x.buf(0), x.c, x.t, true, twy, 1);
   if (!ok) return;
   C* out = b.W2 + f * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < CL::EPT; m++) Store<T>::stc(out + (long long)x.j(m) * g.kxp, Store<T>::ldc(x.at(0, m)));
 }
 
@@ -395,45 +395,73 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     fft_lines<T, CF::H, +1, 1, 0, true>(z, 0, lt, act, twx, 2);
   }
   __syncthreads();
+  constexpr int NQ = INCOMP ? 19 : 11;
+  using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
+  // ---- CFL minimum (vardt, mhd.f90:328-429), screened: every point in FP32, then only the
+  // points within 0.1 % of the block's FP32 minimum (or FP32 NaN) in the state type TS.  The
+  // FP32 value of a point's bound is within 1e-5 of its TS value, so the block's TS minimum
+  // is the one a full TS evaluation gives.
+  if (CFL) {
+    using PHF = typename std::conditional<INCOMP, FluxI<float>, Flux<float>>::type;
+    using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
+    __shared__ float red32[32];
+    const PT<float> pf = pt_float(pc);
+    const float rfac_f = (float)(a.st->radius / a.P.R0);
+    const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
+    auto d32_at = [&](int p) {
+      const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
+      float qf[NQ];
+#pragma unroll
+      for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : 0.f;
+      return PHF::cfl(qf, pf, a.P, rfac_f);
+    };
+    float m32 = __int_as_float(0x7f800000);
+#pragma unroll 1
+    for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) m32 = fminf(m32, d32_at(p));
+    for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
+    if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = m32;
+    __syncthreads();
+    for (int w = 0; w < CF::THREADS / 32; w++) m32 = fminf(m32, red32[w]);
+    const float thr = m32 * 1.001f;
+    TS tmin = Real<TS>::inf();
+    bool nan_seen = false;
+#pragma unroll 1
+    for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
+      const float d32 = d32_at(p);
+      if (!(d32 <= thr) && !isnan(d32)) continue;
+      const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
+      TS qs[NQ];
+#pragma unroll
+      for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : kk.ps.zero;
+      const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
+      if (Real<TS>::isnan_(d)) nan_seen = true;
+      else tmin = Real<TS>::min_(tmin, d);
+    }
+    double dmin = Real<TS>::to_d(tmin);
+    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmin;
+    if (__any_sync(0xffffffffu, nan_seen) && (threadIdx.x & 31) == 0) atomicOr(&a.st->status, LAPS_STATUS_NAN);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = red[0];
+      for (int w = 1; w < CF::THREADS / 32; w++) m = fmin(m, red[w]);
+      atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(m));
+    }
+  }
+  if (nfl == 0) return;
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
-  TS tmin = Real<TS>::inf();
-  bool nan_seen = false;
-  const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
   const T inv_tau = Real<T>::from_d(a.st->inv_tau);
   const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
 #pragma unroll 1
   for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
     int rr = p / NX, xx = row_real_idx(p % NX);
     SR* base = sr + 2 * rr * CF::NF * CF::LC + xx;
-    constexpr int NQ = INCOMP ? 19 : 11;
     T q[NQ];
 #pragma unroll
     for (int f = 0; f < NQ; f++) q[f] = f < nin ? Store<T>::ld(base + 2 * f * CF::LC) : pc.zero;
-    using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
-    using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
-    if (CFL) {  // in the state type: FP64-equivalent even when the transforms run in FP32
-      TS qs[NQ];
-#pragma unroll
-      for (int f = 0; f < NQ; f++) qs[f] = Cvt<TS, T>::r(q[f]);
-      TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
-      if (Real<TS>::isnan_(d)) nan_seen = true;
-      else tmin = Real<TS>::min_(tmin, d);
-    }
-    if (nfl > 0) PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
-  }
-  if (CFL) {
-    double dmin = Real<TS>::to_d(tmin);
-    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmin;
-    if (__any_sync(0xffffffffu, nan_seen) && (threadIdx.x & 31) == 0) atomicOr(&a.st->status, LAPS_STATUS_NAN);
+    PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   __syncthreads();
-  if (CFL && threadIdx.x == 0) {
-    double m = red[0];
-    for (int w = 1; w < CF::THREADS / 32; w++) m = fmin(m, red[w]);
-    atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(m));
-  }
-  if (nfl == 0) return;
   // ---- r2c of the fluxes
   const int sexp = -__ffs(NX) + 1;  // 1/nx
   for (int L0 = 0; L0 < CF::ROWS * nfl; L0 += CF::LB) {
@@ -502,7 +530,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T, TS> b, Pa
   for (int k = 0; k < nin; k++) {
     const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
     const C* in = b.W1 + grp.in[k] * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
       cx<T> v = ok ? Store<T>::ldg(in + (long long)x.j(m) * g.kxp) : cx_zero<T>();
       Store<T>::stc(x.at(bi, m), v);
@@ -583,14 +611,24 @@ struct RkCtx {
     if (P->corot && !plain) return ksq(*K, *P, *pc, rr, kx, ky, kz);
     return (K->kx2[kx] + K->ky2[ky]) + K->kz2[kz];
   }
+  // the RK register of an element as the update needs it: read after stage 0 only (coherent
+  // load: the update rewrites it)
+  __device__ __forceinline__ cx<T> r_of(const typename Store<T>::C* R) const {
+    return stage > 0 ? Store<T>::ldc(R) : cx_zero<T>();
+  }
   __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, typename Store<T>::C* U, typename Store<T>::C* R, T k2,
                                          int kx, int ky, int kz) const {
+    update(v, fnl, u, r_of(R), U, R, k2, kx, ky, kz);
+  }
+  // u: the element's state, r: its RK register (from r_of), both read before the call
+  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, cx<T> r, typename Store<T>::C* U, typename Store<T>::C* R,
+                                         T k2, int kx, int ky, int kz) const {
     const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
     if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - u * (pc->ebm[v] * inv_tau);
     if (mom && P->visc && P->visc_exp) fnl = fnl - u * (pc->nu * k2);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc->eta * k2);
     cx<T> un = fnl * cc + u;
-    if (stage > 0) un = (fnl * cc + Store<T>::ldc(R) * ddc) + u;  // coherent: R is rewritten below
+    if (stage > 0) un = (fnl * cc + r * ddc) + u;
     if (store_rk) Store<T>::stc(R, fnl);
     if (mom && P->visc && !P->visc_exp) {
       T d = ts * k2 * pc->nu + pc->one;
@@ -649,11 +687,11 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, Pa
   // in 2-D, where kz = 0)
   const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
   const int in2 = (v == 6 || a.P.two_d) ? -1 : v == 4 ? 9 : v == 5 ? 8 : v == 7 ? 14 : 2 * v + 1;
-  const int nin = (v == 0 && a.mass_from_state) ? 0 : (in2 < 0 ? 1 : 2);
+  const int nin = in2 < 0 ? 1 : 2;  // (the continuity update from the momentum is k_mass_rk)
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
     const C* in = b.W2 + (k == 0 ? in1 : in2) * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
       cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
       Store<T>::stc(x.at(k, m), w);
@@ -667,18 +705,26 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, Pa
   const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
   CS* U = b.U + v * g.fsc + col;
   CS* R = b.R + v * g.fsc + col;
-#pragma unroll 2
-  for (int m = 0; m < CL::EPT; m++) {
-    int kz = x.j(m);
-    if (!g.kz_in(kz)) continue;
-    const long long idx = kz * zs;
-    cx<TS> fnl;
-    if (nin == 0) {  // continuity: -i k . (rho u)^ from the momentum spectrum (mhdrhs.f90:206-209)
-      TS ax, ay, az;
-      kfac(kk.KS, a.P, kk.ps, rk.rr, kx, ky, kz, ax, ay, az);
-      fnl = -((mul_i(Store<TS>::ldc(b.U + 1 * g.fsc + col + idx), ax) + mul_i(Store<TS>::ldc(b.U + 2 * g.fsc + col + idx), ay)) +
-              mul_i(Store<TS>::ldc(b.U + 3 * g.fsc + col + idx), az));
-    } else {
+  // elements in chunks of CH: the state and RK-register loads of a chunk are issued together
+  // ahead of its arithmetic (the update's stores may alias them as far as the compiler knows)
+  constexpr int CH = CL::EPT < 4 ? CL::EPT : 4;
+#pragma unroll 1
+  for (int m0 = 0; m0 < CL::EPT; m0 += CH) {
+    cx<TS> uo[CH], ro[CH];
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int kz = x.j(m0 + i);
+      const long long idx = kz * zs;
+      const bool in = g.kz_in(kz);
+      uo[i] = in ? Store<TS>::ldc(U + idx) : cx_zero<TS>();
+      ro[i] = in ? rk.r_of(R + idx) : cx_zero<TS>();
+    }
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int m = m0 + i;
+      const int kz = x.j(m);
+      if (!g.kz_in(kz)) continue;
+      const long long idx = kz * zs;
       cx<T> f = Store<T>::ldc(x.at(0, m));
       f = {Real<T>::mul_pow2(f.re, sexp), Real<T>::mul_pow2(f.im, sexp)};
       if (nin > 1) {
@@ -686,10 +732,35 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, Pa
         w = mul_i(cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)}, K.kzd[kz]);
         f = v == 4 ? f + w : f - w;
       }
-      fnl = cvtc<TS>(f);
+      TS k2 = need_k2 ? rk.k2(kx, ky, kz) : kk.ps.zero;
+      rk.update(v, cvtc<TS>(f), uo[i], ro[i], U + idx, R + idx, k2, kx, ky, kz);
     }
-    TS k2 = need_k2 ? rk.k2(kx, ky, kz) : kk.ps.zero;
-    rk.update(v, fnl, Store<TS>::ldc(U + idx), U + idx, R + idx, k2, kx, ky, kz);
+  }
+}
+
+// Continuity update when the mass flux is the momentum (PassArgs::mass_from_state):
+// fnl(rho) = -i k . (rho u)^ read from the state (mhdrhs.f90:206-209), then the tail and the
+// time advance of rho for every kept element.  Launched before pass E updates the momentum.
+template <class T, class TS>
+__global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk) {
+  if (a.st->halt) return;
+  using CS = typename Store<TS>::C;
+  const Geo& g = a.g;
+  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
+  const long long nkx = g.kx_keep, nky = g.nky();
+  const long long tot = nkx * nky * g.nkz();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % nkx);
+    const long long r = i / nkx;
+    const int ky = g.ky_of((int)(r % nky)), kz = g.kz_of((int)(r / nky));
+    const long long idx = ((long long)kz * g.ny + ky) * g.kxp + kx;
+    const cx<TS> m1 = Store<TS>::ldc(b.U + 1 * g.fsc + idx), m2 = Store<TS>::ldc(b.U + 2 * g.fsc + idx),
+                 m3 = Store<TS>::ldc(b.U + 3 * g.fsc + idx);
+    const cx<TS> u0 = Store<TS>::ldc(b.U + idx), r0 = rk.r_of(b.R + idx);
+    TS ax, ay, az;
+    kfac(kk.KS, a.P, kk.ps, rk.rr, kx, ky, kz, ax, ay, az);
+    const cx<TS> fnl = -((mul_i(m1, ax) + mul_i(m2, ay)) + mul_i(m3, az));
+    rk.update(0, fnl, u0, r0, b.U + idx, b.R + idx, kk.ps.zero, kx, ky, kz);
   }
 }
 
@@ -721,7 +792,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
     const C* in = b.W2 + ins[grp][k] * g.fsc + col;
-#pragma unroll 4
+#pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
       cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
       Store<T>::stc(x.at(k, m), w);
