@@ -184,6 +184,23 @@ int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
  * binning of its own.  Either array may be NULL. */
 int laps_spectrum(laps_ctx* ctx, int nshell, double* e_u, double* e_b);
 
+/* Ensembles of independent runs.  No counterpart in the reference (one run per mpirun job):
+ * a batch owns n member contexts on one device, each created from its own laps_params
+ * (grid, variant, precision, eta, nu, d_i, ...), with its own stream, dt, vardt cadence and
+ * status.  laps_batch_step advances every member by nsteps of its own steps by replaying one
+ * CUDA graph per step that forks to all members' streams and joins back, so members of
+ * different sizes run concurrently.  Members are reached through laps_batch_member for
+ * upload, set_time, download, diagnostics; laps_step on a member between batch steps is
+ * allowed, laps_destroy on a member is not (laps_batch_destroy frees them).
+ *   time, dt, status: arrays of n values written after the call (each may be NULL). */
+typedef struct laps_batch laps_batch;
+int laps_batch_create(const laps_params* members, int n, laps_batch** out);
+int laps_batch_size(laps_batch* b);
+int laps_batch_member(laps_batch* b, int i, laps_ctx** ctx);
+int laps_batch_step(laps_batch* b, int nsteps, double* time, double* dt, int* status);
+void laps_batch_destroy(laps_batch* b);
+const char* laps_batch_last_error(laps_batch* b); /* NULL: the last laps_batch_create error */
+
 /* Forward transform of nfields real FP64 fields that allocates no device memory, for hosts
  * that cannot call cudaMalloc (their device memory comes from their own pool or framework,
  * or allocation is not allowed after start-up).  No counterpart in the reference: it is the

@@ -1,8 +1,11 @@
 // C-ABI of the engine (declared in include/laps_gpu.h).  Every entry point converts
 // exceptions into LAPS_E* codes; nothing C++ crosses the boundary.
+#include <chrono>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
+#include <vector>
 #include "engine_impl.cuh"
 
 namespace laps {
@@ -163,5 +166,165 @@ int laps_get_info(laps_ctx* c, laps_info* i) {
   return guarded(c, [&] { c->e->info(i); });
 }
 const char* laps_last_error(laps_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------- ensembles
+// A batch owns n member contexts on one device, each with its own stream.  Its step replays
+// one CUDA graph per step: a fork from the batch's stream to every member's stream, each
+// member's step kernels, and a join back.  Members therefore run concurrently (a 128^2 member
+// alone fills a few SMs) and keep their own dt, cadence and status.
+using laps::Error;  // LAPS_CK throws laps::Error
+
+struct laps_batch {
+  std::vector<laps_ctx*> m;
+  cudaStream_t origin = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+  std::vector<cudaEvent_t> ev_join;
+  int dev = 0;
+  int timeout_ms = 600000;
+  std::string err;
+};
+
+static void batch_free(laps_batch* b) {
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaEvent_t e : b->ev_join) cudaEventDestroy(e);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_done) cudaEventDestroy(b->ev_done);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  for (laps_ctx* c : b->m) laps_destroy(c);
+  delete b;
+}
+
+// bounded wait for everything enqueued on `s` (the same rule as laps_wait)
+static void wait_stream(cudaStream_t s, cudaEvent_t ev, int timeout_ms) {
+  LAPS_CK(cudaEventRecord(ev, s));
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return;
+    if (e != cudaErrorNotReady) throw laps::Error{LAPS_ECUDA, std::string("device error: ") + cudaGetErrorString(e)};
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if (timeout_ms > 0 && ms > timeout_ms) throw laps::Error{LAPS_ETIMEDOUT, "device work did not finish within the timeout"};
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+extern "C" {
+
+int laps_batch_create(const laps_params* members, int n, laps_batch** out) {
+  if (!out) return fail(nullptr, LAPS_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (!members || n < 1 || n > 4096) return fail(nullptr, LAPS_EINVAL, "members must hold 1..4096 parameter sets");
+  for (int i = 1; i < n; i++)
+    if (members[i].device != members[0].device) return fail(nullptr, LAPS_EINVAL, "all members must use one device");
+  laps_batch* b = new (std::nothrow) laps_batch;
+  if (!b) return fail(nullptr, LAPS_ENOMEM, "host allocation failed");
+  b->dev = members[0].device;
+  for (int i = 0; i < n; i++) {
+    laps_ctx* c = nullptr;
+    int rc = laps_create(&members[i], &c);
+    if (rc != LAPS_OK) {
+      std::string m = "member " + std::to_string(i) + ": " + g_create_err;
+      batch_free(b);
+      return fail(nullptr, rc, m);
+    }
+    b->m.push_back(c);
+    if (members[i].timeout_ms > b->timeout_ms) b->timeout_ms = members[i].timeout_ms;
+  }
+  try {
+    LAPS_CK(cudaSetDevice(b->dev));
+    LAPS_CK(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    LAPS_CK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    LAPS_CK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
+    b->ev_join.resize(n, nullptr);
+    for (int i = 0; i < n; i++) LAPS_CK(cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming));
+  } catch (const laps::Error& e) {
+    batch_free(b);
+    return fail(nullptr, e.code, e.msg);
+  }
+  *out = b;
+  return LAPS_OK;
+}
+
+void laps_batch_destroy(laps_batch* b) { batch_free(b); }
+
+int laps_batch_size(laps_batch* b) { return b ? (int)b->m.size() : 0; }
+
+int laps_batch_member(laps_batch* b, int i, laps_ctx** ctx) {
+  if (!b || !ctx) return fail(nullptr, LAPS_EINVAL, "null batch or output pointer");
+  if (i < 0 || i >= (int)b->m.size()) {
+    b->err = "member index out of range";
+    return LAPS_EINVAL;
+  }
+  *ctx = b->m[i];
+  return LAPS_OK;
+}
+
+int laps_batch_step(laps_batch* b, int nsteps, double* time, double* dt, int* status) {
+  if (!b) return fail(nullptr, LAPS_EINVAL, "null batch");
+  if (nsteps < 0) {
+    b->err = "nsteps must be >= 0";
+    return LAPS_EINVAL;
+  }
+  const int n = (int)b->m.size();
+  for (int i = 0; i < n; i++)
+    if (!b->m[i]->e->has_state()) {
+      b->err = "member " + std::to_string(i) + ": no state uploaded";
+      return LAPS_ESTATE;
+    }
+  try {
+    LAPS_CK(cudaSetDevice(b->dev));
+    bool first = false;
+    for (int i = 0; i < n; i++) {
+      b->m[i]->e->reset_flags();
+      first = first || b->m[i]->e->needs_first_step();
+    }
+    int done = 0;
+    if (nsteps > 0 && first) {  // unpruned first steps, each member on its own stream
+      for (int i = 0; i < n; i++) b->m[i]->e->enqueue_one_step();
+      done = 1;
+    }
+    if (done < nsteps) {
+      for (int i = 0; i < n; i++) {  // the graph starts after every member's pending work
+        LAPS_CK(cudaEventRecord(b->ev_join[i], b->m[i]->e->get_stream()));
+        LAPS_CK(cudaStreamWaitEvent(b->origin, b->ev_join[i], 0));
+      }
+      if (!b->graph) {
+        cudaGraph_t gr;
+        LAPS_CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+        LAPS_CK(cudaEventRecord(b->ev_fork, b->origin));
+        for (int i = 0; i < n; i++) {
+          cudaStream_t s = b->m[i]->e->get_stream();
+          LAPS_CK(cudaStreamWaitEvent(s, b->ev_fork, 0));
+          b->m[i]->e->enqueue_one_step();
+          LAPS_CK(cudaEventRecord(b->ev_join[i], s));
+          LAPS_CK(cudaStreamWaitEvent(b->origin, b->ev_join[i], 0));
+        }
+        LAPS_CK(cudaStreamEndCapture(b->origin, &gr));
+        cudaError_t e = cudaGraphInstantiate(&b->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        LAPS_CK(e);
+      }
+      for (; done < nsteps; done++) LAPS_CK(cudaGraphLaunch(b->graph, b->origin));
+      LAPS_CK(cudaEventRecord(b->ev_done, b->origin));
+      for (int i = 0; i < n; i++) LAPS_CK(cudaStreamWaitEvent(b->m[i]->e->get_stream(), b->ev_done, 0));
+    }
+    wait_stream(b->origin, b->ev_done, b->timeout_ms);
+    for (int i = 0; i < n; i++)
+      b->m[i]->e->host_state(time ? time + i : nullptr, dt ? dt + i : nullptr, status ? status + i : nullptr);
+  } catch (const laps::Error& e) {
+    b->err = e.msg;
+    return e.code;
+  } catch (...) {
+    b->err = "unexpected error";
+    return LAPS_ECUDA;
+  }
+  return LAPS_OK;
+}
+
+const char* laps_batch_last_error(laps_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }
 
 }  // extern "C"

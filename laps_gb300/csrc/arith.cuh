@@ -123,11 +123,27 @@ template <> struct Real<float> {
   __device__ __forceinline__ static float sqrt_(float x) { return sqrtf(x); }
   __device__ __forceinline__ static float abs_(float x) { return fabsf(x); }
   __device__ __forceinline__ static float max_(float a, float b) { return (a > b || a != a) ? a : b; }
-  __device__ __forceinline__ static float mul_pow2(float a, int e) { return ldexpf(a, e); }
+  // a * 2^e for |e| < 126 (transform scale factors): one exact multiply
+  __device__ __forceinline__ static float mul_pow2(float a, int e) { return a * __int_as_float((127 + e) << 23); }
   __device__ __forceinline__ static float lead(float x) { return x; }
   __device__ __forceinline__ static bool isnan_(float x) { return x != x; }
   __device__ __forceinline__ static float min_(float a, float b) { return b < a ? b : a; }
   __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
+};
+
+// Division and square root policies of the CFL bound: exact in the arithmetic type, or the
+// approximate FP32 instructions (relative error ~1e-7) for the FP32 screen of pass C.
+template <class T> struct MathExact {
+  __device__ __forceinline__ static T div(T a, T b) { return a / b; }
+  __device__ __forceinline__ static T sqrt(T x) { return Real<T>::sqrt_(x); }
+};
+struct MathFastF {
+  __device__ __forceinline__ static float div(float a, float b) { return __fdividef(a, b); }
+  __device__ __forceinline__ static float sqrt(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
 };
 
 // ------------------------------------------------------------------------------ complex

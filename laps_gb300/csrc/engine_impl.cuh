@@ -60,6 +60,13 @@ class EngineBase {
   virtual void get_time(double* t, double* dt) = 0;
   virtual void info(laps_info* i) = 0;
   virtual void step_profiled(int n, double* pass_ms, double* total_ms, int* status) = 0;
+  // pieces of step() for ensembles, which enqueue several engines' steps into one graph
+  virtual cudaStream_t get_stream() const = 0;
+  virtual bool has_state() const = 0;
+  virtual bool needs_first_step() const = 0;  // the unpruned first step after an upload
+  virtual void reset_flags() = 0;             // clear status and halt (enqueued)
+  virtual void enqueue_one_step() = 0;        // one step, enqueued on get_stream()
+  virtual void host_state(double* time, double* dt, int* status) = 0;  // waits, then reads
 };
 
 // T: compute type of the transforms and products; TS: storage type of the state, the RK
@@ -522,6 +529,21 @@ template <class T, class TS = T> class Engine : public EngineBase {
     read_state();
     return h_st->dt;
   }
+  cudaStream_t get_stream() const override { return stream; }
+  bool has_state() const override { return have_state; }
+  bool needs_first_step() const override { return !dealiased; }
+  void reset_flags() override {
+    LAPS_CK(cudaMemsetAsync(&st->status, 0, sizeof(int), stream));
+    LAPS_CK(cudaMemsetAsync(&st->halt, 0, sizeof(int), stream));
+  }
+  void enqueue_one_step() override { enqueue_step(); }
+  void host_state(double* time, double* dt, int* status) override {
+    read_state();
+    if (time) *time = h_st->time;
+    if (dt) *dt = h_st->dt;
+    if (status) *status = h_st->status;
+  }
+
   void step(int n, double* time, double* dt, int* status) override {
     if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
     LAPS_CK(cudaMemsetAsync(&st->status, 0, sizeof(int), stream));

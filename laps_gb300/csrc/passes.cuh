@@ -225,16 +225,17 @@ struct Flux {
   }
   // min over the axes of dx_i / c_max,i (mhd.f90:355-409; 2-D: x and y only, the
   // explicit-resistivity term and radial x, 2D/mhd.f90:313-392)
+  template <class M = MathExact<T>>
   __device__ __forceinline__ static T cfl(const T* q, const PT<T>& c, const Phys& P, T rfac) {
     const T zero = c.zero, four = c.four, half = c.half;
     const T is2 = c.is2;
-    T rho = q[0], rinv = c.one / rho;
+    T rho = q[0], rinv = M::div(c.one, rho);
     T ux = q[1] * rinv, uy = q[2] * rinv, uz = q[3] * rinv;
     T Bx = q[4], By = q[5], Bz = q[6];
     T p = (q[7] - half * (q[1] * ux + q[2] * uy + q[3] * uz + Bx * Bx + By * By + Bz * Bz)) * c.gm1;
     T cs2 = c.gamma * p * rinv;
-    T sq = Real<T>::sqrt_(rho);
-    T ca[3] = {Bx / sq, By / sq, Bz / sq};
+    T sq = M::sqrt(rho);
+    T ca[3] = {M::div(Bx, sq), M::div(By, sq), M::div(Bz, sq)};
     T u[3] = {ux, uy, uz};
     T ca2 = ca[0] * ca[0] + ca[1] * ca[1] + ca[2] * ca[2];
     T cms2 = cs2 + ca2;
@@ -243,9 +244,9 @@ struct Flux {
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       if (d >= nd) { cmax[d] = c.one; continue; }
-      T cns = Real<T>::sqrt_(Real<T>::max_(cms2 * cms2 - (four * cs2) * (ca[d] * ca[d]), zero));
-      T cf = Real<T>::sqrt_(cms2 + cns) * is2;
-      T cs = Real<T>::sqrt_(Real<T>::max_(cms2 - cns, zero)) * is2;
+      T cns = M::sqrt(Real<T>::max_(cms2 * cms2 - (four * cs2) * (ca[d] * ca[d]), zero));
+      T cf = M::sqrt(cms2 + cns) * is2;
+      T cs = M::sqrt(Real<T>::max_(cms2 - cns, zero)) * is2;
       T m = Real<T>::abs_(u[d] + cf);
       m = Real<T>::max_(m, Real<T>::abs_(u[d] + cs));
       m = Real<T>::max_(m, Real<T>::abs_(u[d] + ca[d]));
@@ -265,11 +266,11 @@ struct Flux {
 #pragma unroll
       for (int d = 0; d < 3; d++) cmax[d] = Real<T>::max_(cmax[d], ch);
     }
-    T dtx = c.dx / cmax[0];
+    T dtx = M::div(c.dx, cmax[0]);
     if (P.zrad) dtx = dtx * rfac;
-    T dty = c.dy / cmax[1] * rfac;
+    T dty = M::div(c.dy, cmax[1]) * rfac;
     if (P.two_d) return Real<T>::min_(dtx, dty);
-    T dtz = c.dz / cmax[2] * rfac;
+    T dtz = M::div(c.dz, cmax[2]) * rfac;
     return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
   }
 };
@@ -302,14 +303,15 @@ struct FluxI {
     out(5, ez);
   }
   // Alfven-only CFL (src_incompressible/mhd.f90:394-463)
+  template <class M = MathExact<T>>
   __device__ __forceinline__ static T cfl(const T* q, const PT<T>& c, const Phys& P, T rfac) {
-    T rho = q[0], rinv = c.one / rho;
+    T rho = q[0], rinv = M::div(c.one, rho);
     T u[3] = {q[1] * rinv, q[2] * rinv, q[3] * rinv};
-    T sq = Real<T>::sqrt_(rho);
+    T sq = M::sqrt(rho);
     T cmax[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      T ca = q[4 + d] / sq;
+      T ca = M::div(q[4 + d], sq);
       T m = Real<T>::abs_(u[d] + ca);
       m = Real<T>::max_(m, Real<T>::abs_(u[d] - ca));
       m = Real<T>::max_(m, Real<T>::abs_(u[d]));
@@ -321,9 +323,9 @@ struct FluxI {
 #pragma unroll
       for (int d = 0; d < 3; d++) cmax[d] = Real<T>::max_(cmax[d], ch);
     }
-    T dtx = c.dx / cmax[0];
-    T dty = c.dy / cmax[1] * rfac;
-    T dtz = c.dz / cmax[2] * rfac;
+    T dtx = M::div(c.dx, cmax[0]);
+    T dty = M::div(c.dy, cmax[1]) * rfac;
+    T dtz = M::div(c.dz, cmax[2]) * rfac;
     return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
   }
 };
@@ -397,10 +399,11 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   __syncthreads();
   constexpr int NQ = INCOMP ? 19 : 11;
   using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
-  // ---- CFL minimum (vardt, mhd.f90:328-429), screened: every point in FP32, then only the
-  // points within 0.1 % of the block's FP32 minimum (or FP32 NaN) in the state type TS.  The
-  // FP32 value of a point's bound is within 1e-5 of its TS value, so the block's TS minimum
-  // is the one a full TS evaluation gives.
+  // ---- CFL minimum (vardt, mhd.f90:328-429), screened: every point in FP32 with the
+  // approximate divide and square root, then only the points within 0.1 % of the block's FP32
+  // minimum (or FP32 NaN) in the state type TS.  The screened value of a point's bound is
+  // within 1e-5 of its TS value, so the block's TS minimum is the one a full TS evaluation
+  // gives.
   if (CFL) {
     using PHF = typename std::conditional<INCOMP, FluxI<float>, Flux<float>>::type;
     using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
@@ -408,16 +411,22 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     const PT<float> pf = pt_float(pc);
     const float rfac_f = (float)(a.st->radius / a.P.R0);
     const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
-    auto d32_at = [&](int p) {
-      const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
-      float qf[NQ];
-#pragma unroll
-      for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : 0.f;
-      return PHF::cfl(qf, pf, a.P, rfac_f);
-    };
+    constexpr int PPT = (CF::ROWS * NX + CF::THREADS - 1) / CF::THREADS;  // points per thread
+    float d32[PPT];
     float m32 = __int_as_float(0x7f800000);
-#pragma unroll 1
-    for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) m32 = fminf(m32, d32_at(p));
+#pragma unroll
+    for (int i = 0; i < PPT; i++) {
+      const int p = threadIdx.x + i * CF::THREADS;
+      d32[i] = m32;
+      if (p < CF::ROWS * NX) {
+        const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
+        float qf[NQ];
+#pragma unroll
+        for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : 0.f;
+        d32[i] = PHF::template cfl<MathFastF>(qf, pf, a.P, rfac_f);
+        m32 = fminf(m32, d32[i]);
+      }
+    }
     for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
     if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = m32;
     __syncthreads();
@@ -426,9 +435,9 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     TS tmin = Real<TS>::inf();
     bool nan_seen = false;
 #pragma unroll 1
-    for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
-      const float d32 = d32_at(p);
-      if (!(d32 <= thr) && !isnan(d32)) continue;
+    for (int i = 0; i < PPT; i++) {
+      const int p = threadIdx.x + i * CF::THREADS;
+      if (p >= CF::ROWS * NX || (!(d32[i] <= thr) && !isnan(d32[i]))) continue;
       const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
       TS qs[NQ];
 #pragma unroll

@@ -102,6 +102,12 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_get_time": (C.c_int, [vp, dp, dp]),
         "laps_get_info": (C.c_int, [vp, P(laps_info)]),
         "laps_last_error": (C.c_char_p, [vp]),
+        "laps_batch_create": (C.c_int, [P(laps_params), C.c_int, P(vp)]),
+        "laps_batch_size": (C.c_int, [vp]),
+        "laps_batch_member": (C.c_int, [vp, C.c_int, P(vp)]),
+        "laps_batch_step": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
+        "laps_batch_destroy": (None, [vp]),
+        "laps_batch_last_error": (C.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -136,14 +142,17 @@ def _dptr(a: np.ndarray):
 class Laps:
     """One GPU run: the reference's hot-path subroutines as methods over a context."""
 
-    def __init__(self, p: laps_params):
+    def __init__(self, p: laps_params, handle=None):
         self.lib = load()
         self.p = p
-        h = C.c_void_p()
-        rc = self.lib.laps_create(C.byref(p), C.byref(h))
-        if rc != LAPS_OK:
-            raise LapsError(rc, self.lib.laps_last_error(None).decode())
-        self.h = h
+        self.owned = handle is None
+        if handle is None:
+            h = C.c_void_p()
+            rc = self.lib.laps_create(C.byref(p), C.byref(h))
+            if rc != LAPS_OK:
+                raise LapsError(rc, self.lib.laps_last_error(None).decode())
+            handle = h
+        self.h = handle
         self.shape = (p.nz, p.ny, p.nx)
 
     def _ck(self, rc):
@@ -152,7 +161,8 @@ class Laps:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.laps_destroy(self.h)
+            if self.owned:
+                self.lib.laps_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -233,3 +243,45 @@ class Laps:
 
     def wait(self, timeout_ms: int = 600000):
         self._ck(self.lib.laps_wait(self.h, int(timeout_ms)))
+
+
+class Batch:
+    """An ensemble of independent runs advanced together (laps_batch_*); members[i] is a Laps
+    view of member i (upload, download, diagnostics), owned by the batch."""
+
+    def __init__(self, plist):
+        self.lib = load()
+        arr = (laps_params * len(plist))(*plist)
+        h = C.c_void_p()
+        rc = self.lib.laps_batch_create(arr, len(plist), C.byref(h))
+        if rc != LAPS_OK:
+            raise LapsError(rc, self.lib.laps_batch_last_error(None).decode())
+        self.h = h
+        self.n = len(plist)
+        self.members = []
+        for i, p in enumerate(plist):
+            m = C.c_void_p()
+            self._ck(self.lib.laps_batch_member(self.h, i, C.byref(m)))
+            self.members.append(Laps(p, handle=m))
+
+    def _ck(self, rc):
+        if rc != LAPS_OK:
+            raise LapsError(rc, self.lib.laps_batch_last_error(self.h).decode())
+
+    def step(self, nsteps: int = 1):
+        """Advance every member by nsteps; returns arrays (time, dt, status)."""
+        t = np.zeros(self.n)
+        d = np.zeros(self.n)
+        s = (C.c_int * self.n)()
+        self._ck(self.lib.laps_batch_step(self.h, int(nsteps), _dptr(t), _dptr(d), s))
+        return t, d, np.array(list(s), dtype=np.int32)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.lib.laps_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -97,3 +97,37 @@ def alfven_wave_ic(n, L=2 * PI, rho0=1.0, p0=0.1, bx0=1.0, db0=0.1, mode=1, cor_
     prim[2] = prim[2] + db0 / sr * c * ca
     prim[5] = prim[5] - db0 * c * ca
     return prim
+
+
+def ensemble_2d(nmembers=64, seed=3, sizes=(128, 256, 512, 1024), kmin=1, kmax=8, rms=0.3):
+    """Members of a 2-D compressible Hall-MHD ensemble with uneven grids and parameters.
+
+    For each member, drawn with ``np.random.default_rng(seed)`` in this order: the grid n
+    (uniform over ``sizes``), eta and nu (log-uniform on [1e-4, 1e-2]), d_i (uniform on
+    [0, 0.1]) and the in-plane field angle theta (uniform on [0, pi/2]).  Returns a list of
+    dicts with ``n``, the ``laps_params`` keyword arguments ``kw`` (variant 2-D compressible,
+    implicit diffusion, 2/3 mask, cfl 0.4, vardt every 20 steps), ``B0`` and the IC ``seed``;
+    ``member_ic(m)`` builds the member's primitive state (random-phase du, db over
+    kmin <= |k| <= kmax with rms ``rms``, rho = 1, p = 0.1).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nmembers):
+        n = int(sizes[rng.integers(len(sizes))])
+        eta = float(10.0 ** rng.uniform(-4.0, -2.0))
+        nu = float(10.0 ** rng.uniform(-4.0, -2.0))
+        di = float(rng.uniform(0.0, 0.1))
+        th = float(rng.uniform(0.0, PI / 2))
+        kw = dict(variant=2, nx=n, ny=n, nz=1, if_resis=1, resistivity=eta, if_visc=1, viscosity=nu,
+                  if_Hall=1 if di > 0 else 0, ion_inertial_length=di, dealias_option=1, cfl=0.4,
+                  dstep_calcdt=20)
+        out.append(dict(n=n, kw=kw, B0=(math.cos(th), math.sin(th), 0.0), seed=1000 * (seed + 1) + i,
+                        kmin=kmin, kmax=kmax, rms=rms))
+    return out
+
+
+def member_ic(m):
+    """Primitive state ``[8, 1, n, n]`` of one ensemble member from ``ensemble_2d``."""
+    n = m["n"]
+    return turbulence_ic((n, n, 1), kmin=m["kmin"], kmax=m["kmax"], alpha=-1.0, rms_u=m["rms"], rms_b=m["rms"],
+                         seed=m["seed"], B0=m["B0"])
