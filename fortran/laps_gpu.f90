@@ -96,6 +96,35 @@ module laps_gpu
             type(c_ptr), value :: ctx
             type(laps_diag), intent(out) :: d
         end function
+        integer(c_int) function laps_spectrum(ctx, nshell, e_u, e_b) bind(C, name='laps_spectrum')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nshell
+            real(c_double), intent(out) :: e_u(*), e_b(*)
+        end function
+        integer(c_int) function laps_batch_create(members, n, batch) bind(C, name='laps_batch_create')
+            import :: c_int, c_ptr, laps_params
+            type(laps_params), intent(in) :: members(*)
+            integer(c_int), value :: n
+            type(c_ptr), intent(out) :: batch
+        end function
+        integer(c_int) function laps_batch_member(batch, i, ctx) bind(C, name='laps_batch_member')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: batch
+            integer(c_int), value :: i
+            type(c_ptr), intent(out) :: ctx
+        end function
+        integer(c_int) function laps_batch_step(batch, nsteps, time, dt, status) bind(C, name='laps_batch_step')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: batch
+            integer(c_int), value :: nsteps
+            real(c_double), intent(out) :: time(*), dt(*)
+            integer(c_int), intent(out) :: status(*)
+        end function
+        subroutine laps_batch_destroy(batch) bind(C, name='laps_batch_destroy')
+            import :: c_ptr
+            type(c_ptr), value :: batch
+        end subroutine
         integer(c_int) function laps_wait(ctx, timeout_ms) bind(C, name='laps_wait')
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx
