@@ -45,7 +45,19 @@ N_GRID = 256
 WORKLOAD = "3D compressible Hall-MHD + expanding box, 256^3"
 CFG2 = dict(if_resis=1, resistivity=5e-4, if_visc=1, viscosity=5e-4, dealias_option=1, cfl=0.4,
             if_Hall=1, ion_inertial_length=0.05, if_AEB=1, radius0=30.0, Ur0=0.3)
+CFG3 = dict(if_resis=1, resistivity=2e-4, if_visc=1, viscosity=2e-4, dealias_option=1, cfl=0.4, rho0=1.0)
 SHAPE = None  # (nx, ny, nz) of a reduced profiling case
+# workloads of the single-run arm: grid, variant, namelist values, description
+WORKLOADS = {
+    "c3d256": dict(grid=256, variant=0, kw=CFG2, label="3D compressible Hall-MHD + expanding box",
+                   data="synthetic (seeded random-phase spectrum, 1<=|k|<=8, rms 0.5, seed 1)",
+                   desc={"variant": "3DC", "hall": 0.05, "expanding_box": "Ur0/R0=0.01", "dealias": "2/3 sphere",
+                         "cfl": 0.4}),
+    "c3di512": dict(grid=512, variant=1, kw=CFG3, label="3D incompressible MHD",
+                    data="synthetic (Taylor-Green-like u, b plus random-phase 1<=|k|<=6, |k|^-5/6, rms 1, seed 2)",
+                    desc={"variant": "3DI", "eta_nu": 2e-4, "dealias": "2/3 sphere", "cfl": 0.4}),
+}
+WL = WORKLOADS["c3d256"]
 # --precision: (C-ABI mode, dtype text, state bytes per complex, work-buffer bytes per complex)
 PRECISIONS = {
     "dd": (1, "f32x2 (float-float)", 16, 16),
@@ -82,9 +94,11 @@ def barrier(ws):
 
 
 def initial_state(n=None):
-    from laps_gb300.ic import turbulence_ic
+    from laps_gb300.ic import taylor_green_ic, turbulence_ic
 
     n = n or (SHAPE if SHAPE else N_GRID)
+    if WL["variant"] == 1:
+        return taylor_green_ic(n, seed=2, kmin=1, kmax=6, alpha=-5.0 / 6.0, rms=1.0)
     return turbulence_ic(n, kmin=1, kmax=8, alpha=-1.0, rms_u=0.5, rms_b=0.5, seed=1)
 
 
@@ -162,6 +176,20 @@ def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, eS=16, eT=16, mass=Tru
     C = n * n * kx_keep * (nin + nfl) * eT
     D = col_B * (nfl * n * eT + nd * nky * eT)
     E = col_A * (nd * n * eT + 8 * nkz * 4 * eS)  # U and R read and written on kept kz
+    return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
+
+
+# the same for the incompressible step: A reads 7 state fields and writes 12 (u, B, J, grad
+# terms), B 12 -> 19, C 19 -> 6 (pressure flux, E), D 6 -> 8, E reads 8 and updates 8 state
+# fields (U and R read and written on kept kz)
+def pass_bytes_3di(n, kx_keep, nky, nkz, eS=16, eT=16):
+    kxp8 = int(math.ceil(kx_keep / 8.0) * 8)
+    col_A, col_B = kxp8 * nky, kxp8 * n
+    A = col_A * (7 * nkz * eS + 12 * n * eT)
+    B = col_B * (12 * nky + 19 * n) * eT
+    C = n * n * kx_keep * 25 * eT
+    D = col_B * (6 * n + 8 * nky) * eT
+    E = col_A * (8 * n * eT + 8 * nkz * 4 * eS)
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 
@@ -324,7 +352,7 @@ def run_ours(args):
     prim = initial_state()
     nx, ny, nz = SHAPE if SHAPE else (n, n, n)
     npts = nx * ny * nz
-    p = ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, device=local, **CFG2)
+    p = ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, device=local, variant=WL["variant"], **WL["kw"])
     g = ffi.Laps(p)
     g.upload_state(prim, primitive=True)
     g.set_time(0.0)
@@ -392,7 +420,8 @@ def run_ours(args):
     # ---- roofline of the dominant pass
     nky, nkz = info.ky_keep, info.kz_keep
     eS, eT = PRECISIONS[args.precision][2:4]
-    pb = pass_bytes(n, info.kx_keep, nky, nkz, eS=eS, eT=eT) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
+    pbf = pass_bytes_3di if WL["variant"] == 1 else pass_bytes
+    pb = pbf(n, info.kx_keep, nky, nkz, eS=eS, eT=eT) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
     launches = args.steps * 3
     dom = max(range(5), key=lambda i: pass_ms[i])
     name = PASS_NAMES[dom]
@@ -410,10 +439,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": PRECISIONS[args.precision][1],
-        "data": "synthetic (seeded random-phase spectrum, 1<=|k|<=8, rms 0.5, seed 1)",
-        "config": {"workload": WORKLOAD, "grid": n, "variant": "3DC", "precision": args.precision, "hall": 0.05,
-                   "expanding_box": "Ur0/R0=0.01", "dealias": "2/3 sphere", "cfl": 0.4,
-                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (7 GB working set)"},
+        "data": WL["data"],
+        "config": dict({"workload": WORKLOAD, "grid": n, "precision": args.precision}, **WL["desc"],
+                       parallelism=f"replicas x{ws}", l2=f"inputs larger than L2 ({info.device_bytes / 1e9:.0f} GB working set)"),
         "gpu_launches": args.steps * info.kernels_per_step,
         "status": status,
         "graph_ms_per_step": graph_ms,
@@ -430,7 +458,7 @@ def run_ours(args):
         line["vs_plain"] = {k: value / v["value"] for k, v in plain.items()}
     if args.precision.startswith("fp32") and not SHAPE and not args.no_err:
         line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and WL["variant"] == 0:
         v, cores, sample = cpu_sample(1, 0)
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
@@ -443,15 +471,16 @@ def run_ours(args):
 
 
 def main():
-    global N_GRID, WORKLOAD
+    global N_GRID, WORKLOAD, WL
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=list(PRECISIONS))
-    ap.add_argument("--workload", default="c3d256", choices=["c3d256", "ens2d"],
-                    help="c3d256: the 3-D Hall + expanding-box case (headline); ens2d: the 2-D ensemble")
+    ap.add_argument("--workload", default="c3d256", choices=["c3d256", "c3di512", "ens2d"],
+                    help="c3d256: the 3-D Hall + expanding-box case (headline); c3di512: the 3-D incompressible "
+                         "FP32-vs-FP64 study at 512^3; ens2d: the 2-D ensemble")
     ap.add_argument("--members", type=int, default=64, help="ensemble members (--workload ens2d)")
     ap.add_argument("--no-plain", action="store_true", dest="no_plain",
                     help="skip timing the plain float-float and FP64 paths beside the headline mode")
@@ -464,12 +493,18 @@ def main():
     ap.add_argument("--shape", default=None, help="nx,ny,nz of a reduced profiling case (overrides --grid)")
     args = ap.parse_args()
     global SHAPE
+    if args.workload in WORKLOADS:
+        WL = WORKLOADS[args.workload]
+        if args.grid == 256 and WL["grid"] != 256:
+            args.grid = WL["grid"]
+        N_GRID = WL["grid"]
+        WORKLOAD = f"{WL['label']}, {N_GRID}^3"
     if args.shape:
         SHAPE = tuple(int(v) for v in args.shape.split(","))
-        WORKLOAD = f"3D compressible Hall-MHD + expanding box, {args.shape} (reduced case)"
+        WORKLOAD = f"{WL['label']}, {args.shape} (reduced case)"
     if args.grid != N_GRID:
         N_GRID = args.grid
-        WORKLOAD = f"3D compressible Hall-MHD + expanding box, {N_GRID}^3 (reduced case)"
+        WORKLOAD = f"{WL['label']}, {N_GRID}^3 (reduced case)"
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "ens2d":

@@ -131,3 +131,38 @@ def member_ic(m):
     n = m["n"]
     return turbulence_ic((n, n, 1), kmin=m["kmin"], kmax=m["kmax"], alpha=-1.0, rms_u=m["rms"], rms_b=m["rms"],
                          seed=m["seed"], B0=m["B0"])
+
+
+def taylor_green_ic(n, seed=2, kmin=1, kmax=6, alpha=-5.0 / 6.0, rms=1.0, rho0=1.0, p0=1.0):
+    """Taylor-Green-like large-scale u and b plus a random-phase component (the 3-D
+    incompressible study case).
+
+    u_TG = (sin x cos y cos z, -cos x sin y cos z, 0) and the divergence-free
+    b_TG = (cos x sin y sin z, sin x cos y sin z, -2 sin x sin y cos z), each scaled to unit
+    rms, plus random-phase divergence-free fields with |k|^alpha amplitudes on
+    kmin <= |k| <= kmax (u drawn first, then b, ``np.random.default_rng(seed)``) of unit rms;
+    the sums are scaled to rms ``rms``.  rho = rho0, p = p0.  Returns ``[8, n, n, n]``.
+    """
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
+    x = np.arange(nx) * (2 * PI / nx)
+    y = np.arange(ny) * (2 * PI / ny)
+    z = np.arange(nz) * (2 * PI / nz)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    sx, cx_, sy, cy, sz, cz = np.sin(X), np.cos(X), np.sin(Y), np.cos(Y), np.sin(Z), np.cos(Z)
+    utg = np.stack([sx * cy * cz, -cx_ * sy * cz, np.zeros_like(X)])
+    btg = np.stack([cx_ * sy * sz, sx * cy * sz, -2.0 * sx * sy * cz])
+
+    def unit(v):
+        return v / math.sqrt(float(np.mean(np.sum(v ** 2, axis=0))))
+
+    rng = np.random.default_rng(seed)
+    du = random_phase_spectrum((nz, ny, nx), (2 * PI,) * 3, kmin, kmax, alpha, rng)
+    db = random_phase_spectrum((nz, ny, nx), (2 * PI,) * 3, kmin, kmax, alpha, rng)
+    u = unit(unit(utg) + du) * rms
+    b = unit(unit(btg) + db) * rms
+    prim = np.empty((8, nz, ny, nx))
+    prim[0] = rho0
+    prim[1:4] = u
+    prim[4:7] = b
+    prim[7] = p0
+    return prim

@@ -193,3 +193,60 @@ def test_dt_floor_stops_without_stepping(prec):
     assert t == 0.0 and dt < 1e-8
     after = g.download_spectral()
     assert np.array_equal(before, after)
+
+
+@pytest.mark.parametrize("prec", [ffi.PREC_DD, ffi.PREC_FP64], ids=["dd", "fp64"])
+@pytest.mark.parametrize("shape", [(512, 16, 8), (16, 512, 8), (16, 8, 512)], ids=["x512", "y512", "z512"])
+def test_long_lines_one_step(prec, shape):
+    """512-point lines along each axis (the 512^3 workloads' transform sizes): one step of the
+    Hall + expanding-box case within 1e-12."""
+    prim = turb(shape, seed=31, kmax=4, rms_u=0.3, rms_b=0.3)
+    o, g = start_pair(shape, CONFIG2, prim, prec)
+    o.dt = 0.0
+    o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    t, dt, status = g.step(1)
+    assert status == 0 and abs(dt - o.dt) <= 1e-13 * o.dt
+    uu, _ = g.download_state()
+    assert rel_l2(uu, o.uu, state_floor(o.uu)).max() < 1e-12
+
+
+@pytest.mark.parametrize("prec", [ffi.PREC_DD, ffi.PREC_FP32], ids=["dd", "fp32"])
+@pytest.mark.parametrize("shape", [(512, 8, 16), (16, 8, 512)], ids=["x512", "z512"])
+def test_long_lines_incompressible(prec, shape):
+    from oracle import laps3d
+
+    kw = dict(if_resis=1, resistivity=2e-4, if_visc=1, viscosity=2e-4, dealias_option=1, cfl=0.4)
+    prim = turb(shape, seed=32, kmax=4, rms_u=0.3, rms_b=0.3, p0=1.0)
+    o = laps3d.restart3di(shape, kw, prim, 0.0)
+    g = ffi.Laps(ffi.params(nx=shape[0], ny=shape[1], nz=shape[2], variant=ffi.VARIANT_3DI, precision=prec, **kw))
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    o.dt = 0.0
+    for _ in range(2):
+        o.step()
+    t, dt, status = g.step(2)
+    assert status == 0
+    uu, _ = g.download_state()
+    tol = 1e-11 if prec == ffi.PREC_DD else 1e-5
+    assert rel_l2(uu, o.uu, state_floor(o.uu)).max() < tol
+
+
+@pytest.mark.parametrize("prec", [ffi.PREC_DD, ffi.PREC_FP32], ids=["dd", "fp32"])
+def test_2d_1024_rows(prec):
+    from oracle import laps3d
+
+    kw = dict(dealias_option=1, cfl=0.4, if_Hall=1, ion_inertial_length=0.05, if_resis=1, resistivity=1e-3,
+              if_visc=1, viscosity=1e-3)
+    prim = turb((1024, 16, 1), seed=33, kmax=6, rms_u=0.3, rms_b=0.3)
+    o = laps3d.restart2d((1024, 16), kw, prim, 0.0)
+    g = ffi.Laps(ffi.params(nx=1024, ny=16, nz=1, variant=ffi.VARIANT_2DC, precision=prec, **kw))
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    o.dt = 0.0
+    for _ in range(3):
+        o.step()
+    t, dt, status = g.step(3)
+    assert status == 0
+    uu, _ = g.download_state()
+    tol = 1e-11 if prec == ffi.PREC_DD else 1e-5
+    assert rel_l2(uu, o.uu, state_floor(o.uu)).max() < tol
