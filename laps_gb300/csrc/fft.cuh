@@ -206,4 +206,75 @@ __device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t,
   }
 }
 
+// Two tiles transformed together (column passes with two inputs): one pass over the stages,
+// the same twiddles applied to both, half the barriers.  FP32 lines only (two 16-element
+// sets of float-float or FP64 values would not fit the register budget); other types
+// transform the two buffers one after the other.
+template <class T, int N, int DIR, int R, int JS>
+__device__ __forceinline__ void fft_stage2(typename Store<T>::C* s0, typename Store<T>::C* s1, int l, int t, int ns, int lns,
+                                           const typename Store<T>::C* __restrict__ tw, int twstep) {
+  using P = Plan<N>;
+  constexpr int NB = P::EPT / R;
+  cx<T> v[2][NB][R];
+  typename Store<T>::C* line0 = s0 + l;
+  typename Store<T>::C* line1 = s1 + l;
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    int b = t + q * P::TPL;
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+      v[0][q][i] = Store<T>::ldc(line0 + sm_idx<JS>(b + i * (N / R)));
+      v[1][q][i] = Store<T>::ldc(line1 + sm_idx<JS>(b + i * (N / R)));
+    }
+    if (ns > 1) {
+      int k = b & (ns - 1);
+      int step = (k * (N / R) >> lns) * twstep;
+#pragma unroll
+      for (int i = 1; i < R; i++) {
+        const cx<T> w = twiddle<T, DIR>(tw, i * step);
+        v[0][q][i] = v[0][q][i] * w;
+        v[1][q][i] = v[1][q][i] * w;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    int b = t + q * P::TPL;
+    int k = b & (ns - 1);
+    dft_r<T, DIR, R>(v[0][q]);
+    dft_r<T, DIR, R>(v[1][q]);
+    int base = ((b >> lns) << lns) * R + k;
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+      Store<T>::stc(line0 + sm_idx<JS>(base + i * ns), v[0][q][i]);
+      Store<T>::stc(line1 + sm_idx<JS>(base + i * ns), v[1][q][i]);
+    }
+  }
+  __syncthreads();
+}
+
+// FFT of the column tiles s0 and, when `both`, s1 (block-uniform); every thread calls it
+template <class T, int N, int DIR, int JS, int LS>
+__device__ __forceinline__ void fft_lines_pair(typename Store<T>::C* s0, typename Store<T>::C* s1, bool both, int l, int t,
+                                               const typename Store<T>::C* __restrict__ tw, int twstep) {
+  using P = Plan<N>;
+  constexpr bool PAIR = sizeof(typename Store<T>::C) == 8 && N >= 16 && LS == 1;
+  if constexpr (PAIR) {
+    if (both) {
+      int ns = 1, lns = 0;
+#pragma unroll 1
+      for (int st = 0; st < P::NS16; st++) {
+        fft_stage2<T, N, DIR, 16, JS>(s0, s1, l, t, ns, lns, tw, twstep);
+        ns <<= 4;
+        lns += 4;
+      }
+      if constexpr (P::REST > 1) fft_stage2<T, N, DIR, P::REST, JS>(s0, s1, l, t, ns, lns, tw, twstep);
+      return;
+    }
+  }
+  fft_lines<T, N, DIR, JS, LS>(s0, l, t, true, tw, twstep);
+  if (both) fft_lines<T, N, DIR, JS, LS>(s1, l, t, true, tw, twstep);
+}
+
 }  // namespace laps

@@ -92,9 +92,34 @@ __device__ __forceinline__ int row_real_idx(int x) { return 2 * sm_idx<1>(x >> 1
 template <class T, int H, class LDX>
 __device__ __forceinline__ void c2r_pre(typename Store<T>::C* z, int t, LDX ldx, const typename Store<T>::C* __restrict__ twx) {
   constexpr int TPL = Plan<H>::TPL;
-  for (int k = t; k <= H / 2; k += TPL) {
+  constexpr int NIT = (H / 2 + TPL) / TPL;  // pairs per thread
+  // FP32 lines: every load of the line's pairs first, then the arithmetic (wider types would
+  // not keep the pairs in registers)
+  constexpr bool HOIST = sizeof(typename Store<T>::C) == 8;
+  cx<T> xa[HOIST ? NIT : 1], xb[HOIST ? NIT : 1];
+  if constexpr (HOIST) {
+#pragma unroll
+    for (int i = 0; i < NIT; i++) {
+      const int k = t + i * TPL;
+      if (k <= H / 2) {
+        xa[i] = ldx(k);
+        xb[i] = ldx(H - k);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NIT; i++) {
+    const int k = t + i * TPL;
+    if (k > H / 2) break;
     int k2 = H - k;
-    cx<T> a = ldx(k), b = ldx(k2);
+    cx<T> a, b;
+    if constexpr (HOIST) {
+      a = xa[i];
+      b = xb[i];
+    } else {
+      a = ldx(k);
+      b = ldx(k2);
+    }
     if (k == 0) { a.im = Real<T>::cst(0.0); b.im = Real<T>::cst(0.0); }
     cx<T> wa = conj(Store<T>::ldg(twx + k));
     cx<T> za = (a + conj(b)) + times_i(wa * (a - conj(b)));

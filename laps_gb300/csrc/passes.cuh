@@ -535,17 +535,33 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T, TS> b, Pa
   const int kind = grp.kind;
   const int nin = grp.in[1] < 0 ? 1 : (grp.in[2] < 0 || (kind == DG_Q8 && !a.aeb) ? 2 : 3);
   C* ob = b.W2 + col + grp.out * g.fsc;
-#pragma unroll 1
-  for (int k = 0; k < nin; k++) {
-    const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
+  // inputs 0 and 1 are loaded together and transformed together; a third goes into the
+  // buffer its group has finished with
+  auto load = [&](int k, int bi) {
     const C* in = b.W1 + grp.in[k] * g.fsc + col;
 #pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
       cx<T> v = ok ? Store<T>::ldg(in + (long long)x.j(m) * g.kxp) : cx_zero<T>();
       Store<T>::stc(x.at(bi, m), v);
     }
+  };
+  // FP32 lines: inputs 0 and 1 loaded together and transformed together; wider types one
+  // input at a time (register budget)
+  constexpr bool PAIR = sizeof(C) == 8;
+  if (PAIR) {
+    load(0, 0);
+    if (nin > 1) load(1, 1);
     __syncthreads();
-    fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
+    fft_lines_pair<T, NY, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twy, 1);
+  }
+#pragma unroll 1
+  for (int k = 0; k < nin; k++) {
+    if (k == 2 || !PAIR) {
+      const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
+      load(k, bi);
+      __syncthreads();
+      fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
+    }
     if (ok) {
 #pragma unroll 2
       for (int m = 0; m < CL::EPT; m++) {
@@ -697,16 +713,26 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, Pa
   const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
   const int in2 = (v == 6 || a.P.two_d) ? -1 : v == 4 ? 9 : v == 5 ? 8 : v == 7 ? 14 : 2 * v + 1;
   const int nin = in2 < 0 ? 1 : 2;  // (the continuity update from the momentum is k_mass_rk)
-#pragma unroll 1
-  for (int k = 0; k < nin; k++) {
+  auto load = [&](int k) {
     const C* in = b.W2 + (k == 0 ? in1 : in2) * g.fsc + col;
 #pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
       cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
       Store<T>::stc(x.at(k, m), w);
     }
+  };
+  if constexpr (sizeof(C) == 8) {  // FP32 lines: both inputs in flight, transformed together
+    load(0);
+    if (nin > 1) load(1);
     __syncthreads();
-    fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
+    fft_lines_pair<T, NZ, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twz, 1);
+  } else {
+#pragma unroll 1
+    for (int k = 0; k < nin; k++) {
+      load(k);
+      __syncthreads();
+      fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
+    }
   }
   if (!ok) return;
   using CS = typename Store<TS>::C;
