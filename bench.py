@@ -175,7 +175,7 @@ def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, eS=16, eT=16, mass=Tru
     B = col_B * (na * nky * eT + nin * n * eT)
     C = n * n * kx_keep * (nin + nfl) * eT
     D = col_B * (nfl * n * eT + nd * nky * eT)
-    E = col_A * (nd * n * eT + 8 * nkz * 4 * eS)  # U and R read and written on kept kz
+    E = col_A * (nd * n * eT + 8 * nkz * 2 * (eS + eT))  # U (state type) and R (work type) read and written
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 
@@ -189,7 +189,7 @@ def pass_bytes_3di(n, kx_keep, nky, nkz, eS=16, eT=16):
     B = col_B * (12 * nky + 19 * n) * eT
     C = n * n * kx_keep * 25 * eT
     D = col_B * (6 * n + 8 * nky) * eT
-    E = col_A * (8 * n * eT + 8 * nkz * 4 * eS)
+    E = col_A * (8 * n * eT + 8 * nkz * 2 * (eS + eT))
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 

@@ -116,7 +116,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
   static long long plan_bytes(const laps_params& q) {
     long long kxp = ((q.nx / 2 + 1) + 7) / 8 * 8;
     long long fsc = kxp * q.ny * q.nz;
-    return (8 + 8) * fsc * (long long)sizeof(CS) + (19 + w2_fields(q)) * fsc * WE + (1 << 20);
+    return 8 * fsc * ((long long)sizeof(CS) + (long long)sizeof(C)) + (19 + w2_fields(q)) * fsc * WE + (1 << 20);
   }
   template <class X> static PT<X> make_pt(const Phys& P) {
     PT<X> c;
@@ -224,12 +224,12 @@ template <class T, class TS = T> class Engine : public EngineBase {
 
     LAPS_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     B.U = dalloc<CS>(8 * g.fsc);
-    B.R = dalloc<CS>(8 * g.fsc);
+    B.R = dalloc<C>(8 * g.fsc);
     B.W1 = (C*)dalloc<unsigned char>(19 * g.fsc * WE);
     B.W2 = (C*)dalloc<unsigned char>(w2_fields(q) * g.fsc * WE);
     bytes = plan_bytes(q) - (1 << 20);
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
-    LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(CS), stream));
+    LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
     auto up = [&](auto* dst, const auto& src) {
       LAPS_CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
     };

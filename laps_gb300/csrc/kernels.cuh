@@ -35,7 +35,7 @@ template <class T, int N> struct Col {
 // float-float)
 template <class T, class TS = T> struct Bufs {
   typename Store<TS>::C* U;  // state spectrum, 8 fields
-  typename Store<TS>::C* R;  // fnl_rk, 8 fields
+  typename Store<T>::C* R;   // fnl_rk, 8 fields (the right-hand side, in the transforms' type)
   typename Store<T>::C* W1;  // work, up to 19 fields
   typename Store<T>::C* W2;  // work, up to 19 fields
 };
@@ -92,34 +92,8 @@ __device__ __forceinline__ int row_real_idx(int x) { return 2 * sm_idx<1>(x >> 1
 template <class T, int H, class LDX>
 __device__ __forceinline__ void c2r_pre(typename Store<T>::C* z, int t, LDX ldx, const typename Store<T>::C* __restrict__ twx) {
   constexpr int TPL = Plan<H>::TPL;
-  constexpr int NIT = (H / 2 + TPL) / TPL;  // pairs per thread
-  // FP32 lines: every load of the line's pairs first, then the arithmetic (wider types would
-  // not keep the pairs in registers)
-  constexpr bool HOIST = sizeof(typename Store<T>::C) == 8;
-  cx<T> xa[HOIST ? NIT : 1], xb[HOIST ? NIT : 1];
-  if constexpr (HOIST) {
-#pragma unroll
-    for (int i = 0; i < NIT; i++) {
-      const int k = t + i * TPL;
-      if (k <= H / 2) {
-        xa[i] = ldx(k);
-        xb[i] = ldx(H - k);
-      }
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < NIT; i++) {
-    const int k = t + i * TPL;
-    if (k > H / 2) break;
-    int k2 = H - k;
-    cx<T> a, b;
-    if constexpr (HOIST) {
-      a = xa[i];
-      b = xb[i];
-    } else {
-      a = ldx(k);
-      b = ldx(k2);
-    }
+  auto pair = [&](int k, cx<T> a, cx<T> b) {
+    const int k2 = H - k;
     if (k == 0) { a.im = Real<T>::cst(0.0); b.im = Real<T>::cst(0.0); }
     cx<T> wa = conj(Store<T>::ldg(twx + k));
     cx<T> za = (a + conj(b)) + times_i(wa * (a - conj(b)));
@@ -131,6 +105,26 @@ __device__ __forceinline__ void c2r_pre(typename Store<T>::C* z, int t, LDX ldx,
       Store<T>::stc(z + sm_idx<1>(k), za);
       if (k2 != k) Store<T>::stc(z + sm_idx<1>(k2), zb);
     }
+  };
+  if constexpr (sizeof(typename Store<T>::C) == 8) {
+    // FP32 lines: every load of the line's pairs first, then the arithmetic
+    constexpr int NIT = (H / 2 + TPL) / TPL;  // pairs per thread
+    cx<T> xa[NIT], xb[NIT];
+#pragma unroll
+    for (int i = 0; i < NIT; i++) {
+      const int k = t + i * TPL;
+      if (k <= H / 2) {
+        xa[i] = ldx(k);
+        xb[i] = ldx(H - k);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NIT; i++) {
+      const int k = t + i * TPL;
+      if (k <= H / 2) pair(k, xa[i], xb[i]);
+    }
+  } else {  // wider types would not keep the pairs in registers
+    for (int k = t; k <= H / 2; k += TPL) pair(k, ldx(k), ldx(H - k));
   }
 }
 

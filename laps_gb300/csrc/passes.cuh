@@ -354,7 +354,7 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int SMEM = ROWS * NF * LC * CB;  // CB: bytes of one complex element
   // resident blocks per SM the register budget is set for: at most 3 (FP32 lines) or 2,
   // within the shared memory and the 2048 threads of an SM
-  static constexpr int OCC0 = CB == 8 ? 3 : 2;
+  static constexpr int OCC0 = CB == 8 ? 4 : 2;
   static constexpr int OCC1 = (227 * 1024) / (SMEM + 1024) < OCC0 ? (227 * 1024) / (SMEM + 1024) : OCC0;
   static constexpr int OCC2 = 2048 / THREADS < OCC1 ? 2048 / THREADS : OCC1;
   static constexpr int OCC = OCC2 < 1 ? 1 : OCC2;
@@ -624,8 +624,12 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T, TS> b, Pa
 // Per-element tail of the spectral right-hand side and the time advance of variable v:
 // expansion damping (mhdrhs.f90:235-251), explicit diffusion (:253-275), the RK3 update with
 // implicit diffusion (rktmod.f90:34-62) and the dealias mask or filter (dealiasing.f90:70-113).
-template <class T>
+// T: the state type (the update's arithmetic); TR: the type of the RK register, which holds
+// the previous stages' right-hand side (the transforms' type: FP32 in the FP32-transform
+// modes, where the right-hand side carries FP32 accuracy anyway)
+template <class T, class TR = T>
 struct RkCtx {
+  using CR = typename Store<TR>::C;
   const Geo* g;
   const Phys* P;
   const PT<T>* pc;
@@ -638,23 +642,23 @@ struct RkCtx {
   }
   // the RK register of an element as the update needs it: read after stage 0 only (coherent
   // load: the update rewrites it)
-  __device__ __forceinline__ cx<T> r_of(const typename Store<T>::C* R) const {
-    return stage > 0 ? Store<T>::ldc(R) : cx_zero<T>();
+  __device__ __forceinline__ cx<T> r_of(const CR* R) const {
+    return stage > 0 ? cvtc<T>(Store<TR>::ldc(R)) : cx_zero<T>();
   }
-  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, typename Store<T>::C* U, typename Store<T>::C* R, T k2,
-                                         int kx, int ky, int kz) const {
+  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, typename Store<T>::C* U, CR* R, T k2, int kx, int ky,
+                                         int kz) const {
     update(v, fnl, u, r_of(R), U, R, k2, kx, ky, kz);
   }
   // u: the element's state, r: its RK register (from r_of), both read before the call
-  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, cx<T> r, typename Store<T>::C* U, typename Store<T>::C* R,
-                                         T k2, int kx, int ky, int kz) const {
+  __device__ __forceinline__ void update(int v, cx<T> fnl, cx<T> u, cx<T> r, typename Store<T>::C* U, CR* R, T k2, int kx,
+                                         int ky, int kz) const {
     const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
     if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - u * (pc->ebm[v] * inv_tau);
     if (mom && P->visc && P->visc_exp) fnl = fnl - u * (pc->nu * k2);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc->eta * k2);
     cx<T> un = fnl * cc + u;
     if (stage > 0) un = (fnl * cc + r * ddc) + u;
-    if (store_rk) Store<T>::stc(R, fnl);
+    if (store_rk) Store<TR>::stc(R, cvtc<TR>(fnl));
     if (mom && P->visc && !P->visc_exp) {
       T d = ts * k2 * pc->nu + pc->one;
       un = {un.re / d, un.im / d};
@@ -672,9 +676,9 @@ struct RkCtx {
   }
 };
 
-template <class T>
-__device__ __forceinline__ RkCtx<T> rk_ctx(const PassArgs& a, const PT<T>& pc, const KTab<T>& K) {
-  RkCtx<T> r;
+template <class TR, class T>
+__device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& pc, const KTab<T>& K) {
+  RkCtx<T, TR> r;
   r.g = &a.g; r.P = &a.P; r.pc = &pc; r.K = &K;
   r.stage = a.stage;
   r.store_rk = a.store_rk;
@@ -736,10 +740,10 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, Pa
   }
   if (!ok) return;
   using CS = typename Store<TS>::C;
-  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
+  const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
   const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
   CS* U = b.U + v * g.fsc + col;
-  CS* R = b.R + v * g.fsc + col;
+  C* R = b.R + v * g.fsc + col;
   // elements in chunks of CH: the state and RK-register loads of a chunk are issued together
   // ahead of its arithmetic (the update's stores may alias them as far as the compiler knows)
   constexpr int CH = CL::EPT < 4 ? CL::EPT : 4;
@@ -781,7 +785,7 @@ __global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, Pass
   if (a.st->halt) return;
   using CS = typename Store<TS>::C;
   const Geo& g = a.g;
-  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
+  const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
   const long long nkx = g.kx_keep, nky = g.nky();
   const long long tot = nkx * nky * g.nkz();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
@@ -837,7 +841,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
   }
   if (!ok) return;
   using CS = typename Store<TS>::C;
-  const RkCtx<TS> rk = rk_ctx(a, kk.ps, kk.KS);
+  const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
   const T rr = Real<T>::from_d(a.st->r_ratio);
 #pragma unroll 1
   for (int m = 0; m < CL::EPT; m++) {
