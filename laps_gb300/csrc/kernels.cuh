@@ -128,6 +128,60 @@ __device__ __forceinline__ void c2r_pre(typename Store<T>::C* z, int t, LDX ldx,
   }
 }
 
+// Two real rows a, b as one complex line z = x_a + i x_b, from their half spectra X_a, X_b
+// (read for k < kk, zero beyond): Z[k] = X_a[k] + i X_b[k] and Z[N-k] = conj X_a[k] + i conj X_b[k]
+// for 0 < k < N/2; the imaginary parts of the k = 0 and k = N/2 terms are dropped (the c2r of
+// fftw.f90:73-103 ignores them).  The unnormalised inverse FFT of Z then gives both rows.
+template <class T, int N>
+__device__ __forceinline__ void pair_c2r(typename Store<T>::C* z, int t, int kk, const typename Store<T>::C* __restrict__ xa,
+                                         const typename Store<T>::C* __restrict__ xb) {
+  constexpr int TPL = Plan<N>::TPL;
+  auto put = [&](int k, cx<T> a, cx<T> b) {
+    if (k == 0 || 2 * k == N) {
+      Store<T>::stc(z + sm_idx<1>(k), cx<T>{a.re, b.re});
+    } else {
+      Store<T>::stc(z + sm_idx<1>(k), cx<T>{a.re - b.im, a.im + b.re});
+      Store<T>::stc(z + sm_idx<1>(N - k), cx<T>{a.re + b.im, b.re - a.im});
+    }
+  };
+  if constexpr (sizeof(typename Store<T>::C) == 8) {  // FP32 lines: all loads first
+    constexpr int NIT = (N / 2 + TPL) / TPL;
+    cx<T> va[NIT], vb[NIT];
+#pragma unroll
+    for (int i = 0; i < NIT; i++) {
+      const int k = t + i * TPL;
+      const bool in = k <= N / 2 && k < kk;
+      va[i] = in ? Store<T>::ldg(xa + k) : cx_zero<T>();
+      vb[i] = in ? Store<T>::ldg(xb + k) : cx_zero<T>();
+    }
+#pragma unroll
+    for (int i = 0; i < NIT; i++) {
+      const int k = t + i * TPL;
+      if (k <= N / 2) put(k, va[i], vb[i]);
+    }
+  } else {
+    for (int k = t; k <= N / 2; k += TPL) {
+      const bool in = k < kk;
+      put(k, in ? Store<T>::ldg(xa + k) : cx_zero<T>(), in ? Store<T>::ldg(xb + k) : cx_zero<T>());
+    }
+  }
+}
+
+// The two rows' half spectra from the forward FFT Z of z = x_a + i x_b:
+// X_a[k] = (Z[k] + conj Z[N-k]) / 2, X_b[k] = (Z[k] - conj Z[N-k]) / 2i, each times 2^scale_exp,
+// written for k < kk (k <= N/2).
+template <class T, int N>
+__device__ __forceinline__ void pair_r2c(const typename Store<T>::C* z, int t, int kk, typename Store<T>::C* xa,
+                                         typename Store<T>::C* xb, int scale_exp) {
+  constexpr int TPL = Plan<N>::TPL;
+  for (int k = t; k <= N / 2 && k < kk; k += TPL) {
+    const cx<T> A = Store<T>::ldc(z + sm_idx<1>(k)), B = Store<T>::ldc(z + sm_idx<1>((N - k) & (N - 1)));
+    const cx<T> s = {A.re + B.re, A.im - B.im}, d = {A.im + B.im, B.re - A.re};
+    Store<T>::stc(xa + k, cx<T>{Real<T>::mul_pow2(s.re, scale_exp - 1), Real<T>::mul_pow2(s.im, scale_exp - 1)});
+    Store<T>::stc(xb + k, cx<T>{Real<T>::mul_pow2(d.re, scale_exp - 1), Real<T>::mul_pow2(d.im, scale_exp - 1)});
+  }
+}
+
 // r2c post-processing of one line: X[k] = (Z[k] + conj Z[h-k])/2 - i W^k (Z[k] - conj Z[h-k])/2,
 // X[0] = Re Z0 + Im Z0, X[h] = Re Z0 - Im Z0; each result times 2^scale_exp, handed to `stx`.
 template <class T, int H, class STX>

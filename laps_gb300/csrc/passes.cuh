@@ -351,7 +351,15 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int LB = ONE_ROW ? 12 : 24 * MUL;  // lines per batch
   static constexpr int THREADS = LB * TPL;
   static constexpr int ROWS = ONE_ROW ? 1 : 2 * MUL;
-  static constexpr int SMEM = ROWS * NF * LC * CB;  // CB: bytes of one complex element
+  // Paired rows: rows 2p and 2p+1 of a field share one complex line of NX points,
+  // z = x_2p + i x_2p+1, so a row pair takes one full-length complex FFT and no twiddled
+  // packing; lines of more than one warp (NX = 1024) keep the half-length form.
+  static constexpr int TPLP = Plan<NX>::TPL;
+  static constexpr bool PAIRED = !ONE_ROW && TPLP <= 32;
+  static constexpr int LCP = RowLen<NX>::V;   // padded complex per paired line
+  static constexpr int LBP = THREADS / TPLP;  // paired lines per batch
+  static constexpr int FSTR = PAIRED ? 2 * LCP : 2 * LC;  // field stride in reals
+  static constexpr int SMEM = (PAIRED ? (ROWS / 2) * NF * LCP : ROWS * NF * LC) * CB;  // CB: bytes of one complex
   // resident blocks per SM the register budget is set for: at most 3 (FP32 lines) or 2,
   // within the shared memory and the 2048 threads of an SM
   static constexpr int OCC0 = CB == 8 ? 4 : 2;
@@ -381,20 +389,44 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   const int nfl = a.cfl == 2 ? 0 : (INCOMP ? 6 : (a.mass_from_state ? 13 : 16) - (a.aeb ? 0 : 1));
   long long row0 = (long long)blockIdx.x * CF::ROWS;  // row = z*ny + y
   const int lt = threadIdx.x % CF::TPL, lb = threadIdx.x / CF::TPL;
-  // ---- c2r of the inputs
-  for (int L0 = 0; L0 < CF::ROWS * nin; L0 += CF::LB) {
-    int L = L0 + lb;
-    bool act = L < CF::ROWS * nin;
-    int rr = act ? L / nin : 0, f = act ? L % nin : 0;
-    C* z = sc + (rr * CF::NF + f) * CF::LC;
-    if (act) {
-      const C* xin = b.W2 + f * g.fsc + (row0 + rr) * g.kxp;
-      int kk = g.kx_keep;
-      c2r_pre<T, CF::H>(z, lt, [&](int k) { return k < kk ? Store<T>::ldg(xin + k) : cx_zero<T>(); }, twx);
+  // real values of point p (row p / NX, x = p % NX): field f at base + f * CF::FSTR
+  auto point_base = [&](int p) -> SR* {
+    const int rr = p / NX, x = p % NX;
+    if constexpr (CF::PAIRED) return sr + 2 * ((rr >> 1) * CF::NF * CF::LCP + sm_idx<1>(x)) + (rr & 1);
+    else return sr + 2 * rr * CF::NF * CF::LC + row_real_idx(x);
+  };
+  const int kk_in = g.kx_keep;
+  if constexpr (CF::PAIRED) {
+    // ---- inverse x-transform of row pairs: Z = X_a + i X_b over the full line (the
+    // imaginary parts of the DC and Nyquist terms are dropped, as the reference's c2r does)
+    const int ltp = threadIdx.x % CF::TPLP, lbp = threadIdx.x / CF::TPLP;
+    constexpr int NPAIR = CF::ROWS / 2;
+    for (int L0 = 0; L0 < NPAIR * nin; L0 += CF::LBP) {
+      const int L = L0 + lbp;
+      const bool act = L < NPAIR * nin;
+      const int pr = act ? L / nin : 0, f = act ? L % nin : 0;
+      C* z = sc + (pr * CF::NF + f) * CF::LCP;
+      if (act) {
+        const C* xa = b.W2 + f * g.fsc + (row0 + 2 * pr) * g.kxp;
+        pair_c2r<T, NX>(z, ltp, kk_in, xa, xa + g.kxp);
+      }
+      __syncwarp();  // a line and its threads stay within one warp until the physics
+      fft_lines<T, NX, +1, 1, 0, true>(z, 0, ltp, act, twx, 1);
     }
-    // a line and its threads stay within one warp until the physics reads across lines
-    __syncwarp();
-    fft_lines<T, CF::H, +1, 1, 0, true>(z, 0, lt, act, twx, 2);
+  } else {
+    // ---- c2r of the inputs, one half-length complex line per row
+    for (int L0 = 0; L0 < CF::ROWS * nin; L0 += CF::LB) {
+      int L = L0 + lb;
+      bool act = L < CF::ROWS * nin;
+      int rr = act ? L / nin : 0, f = act ? L % nin : 0;
+      C* z = sc + (rr * CF::NF + f) * CF::LC;
+      if (act) {
+        const C* xin = b.W2 + f * g.fsc + (row0 + rr) * g.kxp;
+        c2r_pre<T, CF::H>(z, lt, [&](int k) { return k < kk_in ? Store<T>::ldg(xin + k) : cx_zero<T>(); }, twx);
+      }
+      __syncwarp();  // a line and its threads stay within one warp until the physics
+      fft_lines<T, CF::H, +1, 1, 0, true>(z, 0, lt, act, twx, 2);
+    }
   }
   __syncthreads();
   constexpr int NQ = INCOMP ? 19 : 11;
@@ -419,10 +451,10 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       const int p = threadIdx.x + i * CF::THREADS;
       d32[i] = m32;
       if (p < CF::ROWS * NX) {
-        const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
+        const SR* base = point_base(p);
         float qf[NQ];
 #pragma unroll
-        for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : 0.f;
+        for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + f * CF::FSTR)) : 0.f;
         d32[i] = PHF::template cfl<MathFastF>(qf, pf, a.P, rfac_f);
         m32 = fminf(m32, d32[i]);
       }
@@ -438,10 +470,10 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     for (int i = 0; i < PPT; i++) {
       const int p = threadIdx.x + i * CF::THREADS;
       if (p >= CF::ROWS * NX || (!(d32[i] <= thr) && !isnan(d32[i]))) continue;
-      const SR* base = sr + 2 * (p / NX) * CF::NF * CF::LC + row_real_idx(p % NX);
+      const SR* base = point_base(p);
       TS qs[NQ];
 #pragma unroll
-      for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(base + 2 * f * CF::LC)) : kk.ps.zero;
+      for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(base + f * CF::FSTR)) : kk.ps.zero;
       const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
       if (Real<TS>::isnan_(d)) nan_seen = true;
       else tmin = Real<TS>::min_(tmin, d);
@@ -463,26 +495,40 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
 #pragma unroll 1
   for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
-    int rr = p / NX, xx = row_real_idx(p % NX);
-    SR* base = sr + 2 * rr * CF::NF * CF::LC + xx;
+    SR* base = point_base(p);
     T q[NQ];
 #pragma unroll
-    for (int f = 0; f < NQ; f++) q[f] = f < nin ? Store<T>::ld(base + 2 * f * CF::LC) : pc.zero;
-    PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + 2 * k * CF::LC, v); }, pc, a.P, inv_tau, inv_rho0);
+    for (int f = 0; f < NQ; f++) q[f] = f < nin ? Store<T>::ld(base + f * CF::FSTR) : pc.zero;
+    PH::eval(q, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::st(base + k * CF::FSTR, v); }, pc, a.P, inv_tau, inv_rho0);
   }
   __syncthreads();
-  // ---- r2c of the fluxes
+  // ---- forward x-transforms of the fluxes
   const int sexp = -__ffs(NX) + 1;  // 1/nx
-  for (int L0 = 0; L0 < CF::ROWS * nfl; L0 += CF::LB) {
-    int L = L0 + lb;
-    bool act = L < CF::ROWS * nfl;
-    int rr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
-    C* z = sc + (rr * CF::NF + f) * CF::LC;
-    fft_lines<T, CF::H, -1, 1, 0, true>(z, 0, lt, act, twx, 2);
-    if (act) {
-      C* xo = b.W1 + f * g.fsc + (row0 + rr) * g.kxp;
-      int kk = g.kx_keep;
-      r2c_post<T, CF::H>(z, lt, [&](int k, cx<T> v) { if (k < kk) Store<T>::stc(xo + k, v); }, sexp, twx);
+  if constexpr (CF::PAIRED) {
+    const int ltp = threadIdx.x % CF::TPLP, lbp = threadIdx.x / CF::TPLP;
+    constexpr int NPAIR = CF::ROWS / 2;
+    for (int L0 = 0; L0 < NPAIR * nfl; L0 += CF::LBP) {
+      const int L = L0 + lbp;
+      const bool act = L < NPAIR * nfl;
+      const int pr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
+      C* z = sc + (pr * CF::NF + f) * CF::LCP;
+      fft_lines<T, NX, -1, 1, 0, true>(z, 0, ltp, act, twx, 1);
+      if (act) {
+        C* xa = b.W1 + f * g.fsc + (row0 + 2 * pr) * g.kxp;
+        pair_r2c<T, NX>(z, ltp, kk_in, xa, xa + g.kxp, sexp);
+      }
+    }
+  } else {
+    for (int L0 = 0; L0 < CF::ROWS * nfl; L0 += CF::LB) {
+      int L = L0 + lb;
+      bool act = L < CF::ROWS * nfl;
+      int rr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
+      C* z = sc + (rr * CF::NF + f) * CF::LC;
+      fft_lines<T, CF::H, -1, 1, 0, true>(z, 0, lt, act, twx, 2);
+      if (act) {
+        C* xo = b.W1 + f * g.fsc + (row0 + rr) * g.kxp;
+        r2c_post<T, CF::H>(z, lt, [&](int k, cx<T> v) { if (k < kk_in) Store<T>::stc(xo + k, v); }, sexp, twx);
+      }
     }
   }
 }
