@@ -34,9 +34,14 @@ def _newest_dep() -> float:
     return max(p.stat().st_mtime for p in deps)
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> Path:
+def build(verbose: bool = False, jobs: int | None = None, extra_flags=(), build_dir: Path | None = None,
+          lib: Path | None = None) -> Path:
+    """Compile and link; ``extra_flags`` (e.g. ``-DNAME=VALUE`` tuning macros) go to every nvcc
+    call, ``build_dir`` / ``lib`` redirect the objects and the library (another variant)."""
     nvcc = _nvcc()
-    BUILD.mkdir(exist_ok=True)
+    BUILD = Path(build_dir) if build_dir else PKG / "_build"
+    LIB = Path(lib) if lib else PKG / "liblaps_gpu.so"
+    BUILD.mkdir(parents=True, exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu"))
     dep_t = _newest_dep()
     todo = []
@@ -47,7 +52,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
 
     def compile_one(so):
         s, o = so
-        cmd = [nvcc, *FLAGS, *ARCH, "-c", str(s), "-o", str(o)]
+        cmd = [nvcc, *FLAGS, *extra_flags, *ARCH, "-c", str(s), "-o", str(o)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {s.name}:\n{r.stderr[-4000:]}")

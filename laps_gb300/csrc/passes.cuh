@@ -533,6 +533,14 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   }
 }
 
+// Resident blocks per SM the register budget of passes D and E is set for (FP32 lines): 5
+// measured best at 256^3 (1, no bound: +3 % step time; 6 and 7 spill: +9 %, +11 %);
+// LAPS_MINB_COL overrides it at build time for tuning sweeps.
+#ifndef LAPS_MINB_COL
+#define LAPS_MINB_COL 5
+#endif
+template <class T> struct ColOcc { static constexpr int V = sizeof(typename Store<T>::C) == 8 ? LAPS_MINB_COL : 1; };
+
 // ============================================================================ pass D
 // forward y-FFT of the fluxes with the kx, ky parts of the spectral right-hand side folded
 // in (calc_rhs, mhdrhs.f90:206-233), leaving only the kz parts for pass E.  Compressible
@@ -562,7 +570,7 @@ __constant__ DGroup c_dgroups[2][8] = {
      {{5, -1, -1}, DG_EZ, 6}}};
 
 template <class T, class TS, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
+__global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V) k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NY>;
@@ -741,7 +749,7 @@ __device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& p
 // the time advance of variable v = blockIdx.z.  Tile: kx0..kx0+7, one kept ky row; reads all
 // z of W2, writes kept kz of U (and R).
 template <class T, class TS, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V) k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;

@@ -71,11 +71,13 @@ _lib = None
 
 
 def load(path: str | os.PathLike | None = None) -> C.CDLL:
-    """Load ``liblaps_gpu.so`` (building it first when it is missing)."""
+    """Load ``liblaps_gpu.so`` (building it first when it is missing); ``LAPS_GPU_LIB`` in the
+    environment names another build of the library."""
     global _lib
     if _lib is not None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    env = os.environ.get("LAPS_GPU_LIB")
+    p = Path(path) if path else (Path(env) if env else LIB_PATH)
     if not p.exists():
         from . import build as _b
         _b.build()
