@@ -184,6 +184,16 @@ int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
  * binning of its own.  Either array may be NULL. */
 int laps_spectrum(laps_ctx* ctx, int nshell, double* e_u, double* e_b);
 
+/* The reference's output / restart file outNNN.dat (mhdoutput.f90:72-131, restart.f90:17-63):
+ * a Fortran unformatted record with the time as a 4-byte real (12 bytes with its markers),
+ * then uu(nx,ny,nz,8) as 8-byte reals in Fortran order.  laps_write_output writes the current
+ * state and time (LAPS_LAYOUT_PRIMITIVE: rho, u, B, p as the reference's output_uu does;
+ * LAPS_LAYOUT_CONSERVED: the conserved state), copying through page-locked buffers with the
+ * device-to-host copies overlapped with the file writes.  laps_read_restart reads such a file
+ * (primitive), uploads it and sets the time, which the file holds as a 4-byte real. */
+int laps_write_output(laps_ctx* ctx, const char* path, int layout);
+int laps_read_restart(laps_ctx* ctx, const char* path, double* time);
+
 /* Ensembles of independent runs.  No counterpart in the reference (one run per mpirun job):
  * a batch owns n member contexts on one device, each created from its own laps_params
  * (grid, variant, precision, eta, nu, d_i, ...), with its own stream, dt, vardt cadence and

@@ -1,6 +1,8 @@
 // C-ABI of the engine (declared in include/laps_gpu.h).  Every entry point converts
 // exceptions into LAPS_E* codes; nothing C++ crosses the boundary.
 #include <chrono>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -326,5 +328,126 @@ int laps_batch_step(laps_batch* b, int nsteps, double* time, double* dt, int* st
 }
 
 const char* laps_batch_last_error(laps_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------- output files
+// The reference's outNNN.dat (mhdoutput.f90:72-131, restart.f90:17-63): a Fortran unformatted
+// sequential record holding the time as a 4-byte real (4-byte length markers: 12 bytes), then
+// uu(nx,ny,nz,8) as 8-byte reals in Fortran order from byte 12 (the MPI-IO view's displacement;
+// the reference is built with -r8).  Primitive output replaces rho u by u and, in the
+// compressible codes, e by p; the incompressible state already holds p.
+
+namespace {
+
+struct PinnedPair {  // two page-locked bounce buffers for overlapped copies and file I/O
+  double* buf[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  explicit PinnedPair(size_t n) {
+    for (int i = 0; i < 2; i++) {
+      LAPS_CK(cudaMallocHost(&buf[i], n * sizeof(double)));
+      LAPS_CK(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+    }
+  }
+  ~PinnedPair() {
+    for (int i = 0; i < 2; i++) {
+      if (buf[i]) cudaFreeHost(buf[i]);
+      if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+  }
+};
+
+void wait_event(cudaEvent_t ev, int timeout_ms) {
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return;
+    if (e != cudaErrorNotReady) throw laps::Error{LAPS_ECUDA, std::string("device error: ") + cudaGetErrorString(e)};
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if (timeout_ms > 0 && ms > timeout_ms) throw laps::Error{LAPS_ETIMEDOUT, "device work did not finish within the timeout"};
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+struct File {
+  FILE* f = nullptr;
+  File(const char* path, const char* mode) : f(std::fopen(path, mode)) {}
+  ~File() {
+    if (f) std::fclose(f);
+  }
+};
+
+constexpr size_t kChunk = size_t(1) << 22;  // doubles per bounce buffer (32 MiB)
+
+}  // namespace
+
+extern "C" {
+
+int laps_write_output(laps_ctx* c, const char* path, int layout) {
+  if (!path) return fail(c, LAPS_EINVAL, "null path");
+  if (layout != LAPS_LAYOUT_PRIMITIVE && layout != LAPS_LAYOUT_CONSERVED) return fail(c, LAPS_EINVAL, "bad layout");
+  return guarded(c, [&] {
+    laps::EngineBase* e = c->e;
+    double t = 0.0, dt = 0.0;
+    e->get_time(&t, &dt);
+    const double* dev = e->stage_real_state();
+    const long long n = e->grid_points();
+    cudaStream_t s = e->get_stream();
+    File out(path, "wb");
+    if (!out.f) throw laps::Error{LAPS_EINVAL, std::string("cannot open ") + path + " for writing"};
+    const int32_t mark = 4;
+    const float t4 = (float)t;
+    bool ok = std::fwrite(&mark, 4, 1, out.f) == 1 && std::fwrite(&t4, 4, 1, out.f) == 1 && std::fwrite(&mark, 4, 1, out.f) == 1;
+    // field f of the file: conserved slot f, or u (prim 0..2) for slots 1..3 and p (prim 3)
+    // for slot 7 of the compressible codes
+    const bool prim = layout == LAPS_LAYOUT_PRIMITIVE;
+    const bool incomp = e->variant() == LAPS_VARIANT_3DI;
+    auto src = [&](int f) -> const double* {
+      if (prim && f >= 1 && f <= 3) return dev + (8 + f - 1) * n;
+      if (prim && f == 7 && !incomp) return dev + 11 * n;
+      return dev + (long long)f * n;
+    };
+    PinnedPair pp((size_t)std::min<long long>(n * 8, (long long)kChunk));
+    // chunks over the 8 fields; the copy of chunk i+1 runs while chunk i is written
+    struct Piece { const double* p; size_t cnt; };
+    std::vector<Piece> pieces;
+    for (int f = 0; f < 8; f++)
+      for (long long o = 0; o < n; o += (long long)kChunk) pieces.push_back({src(f) + o, (size_t)std::min<long long>(kChunk, n - o)});
+    auto issue = [&](size_t i) {
+      const int b = (int)(i & 1);
+      LAPS_CK(cudaMemcpyAsync(pp.buf[b], pieces[i].p, pieces[i].cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+      LAPS_CK(cudaEventRecord(pp.ev[b], s));
+    };
+    if (!pieces.empty()) issue(0);
+    for (size_t i = 0; i < pieces.size(); i++) {
+      const int b = (int)(i & 1);
+      wait_event(pp.ev[b], 600000);
+      if (i + 1 < pieces.size()) issue(i + 1);
+      ok = ok && std::fwrite(pp.buf[b], sizeof(double), pieces[i].cnt, out.f) == pieces[i].cnt;
+    }
+    if (!ok) throw laps::Error{LAPS_EINVAL, std::string("write failed: ") + path};
+  });
+}
+
+int laps_read_restart(laps_ctx* c, const char* path, double* time) {
+  if (!path) return fail(c, LAPS_EINVAL, "null path");
+  return guarded(c, [&] {
+    laps::EngineBase* e = c->e;
+    const long long n = e->grid_points();
+    File in(path, "rb");
+    if (!in.f) throw laps::Error{LAPS_EINVAL, std::string("cannot open ") + path};
+    int32_t m0 = 0, m1 = 0;
+    float t4 = 0.f;
+    if (std::fread(&m0, 4, 1, in.f) != 1 || std::fread(&t4, 4, 1, in.f) != 1 || std::fread(&m1, 4, 1, in.f) != 1 || m0 != 4 || m1 != 4)
+      throw laps::Error{LAPS_EINVAL, std::string("not an output file (bad time record): ") + path};
+    std::vector<double> uu((size_t)n * 8);
+    if (std::fread(uu.data(), sizeof(double), uu.size(), in.f) != uu.size())
+      throw laps::Error{LAPS_EINVAL, std::string("output file too short for this grid: ") + path};
+    e->upload(uu.data(), LAPS_LAYOUT_PRIMITIVE);
+    const double t = (double)t4;  // the restart time goes through a 4-byte real
+    e->set_time(t);
+    if (time) *time = t;
+  });
+}
 
 }  // extern "C"

@@ -67,6 +67,11 @@ class EngineBase {
   virtual void reset_flags() = 0;             // clear status and halt (enqueued)
   virtual void enqueue_one_step() = 0;        // one step, enqueued on get_stream()
   virtual void host_state(double* time, double* dt, int* status) = 0;  // waits, then reads
+  // the real state in the reference's order on the device (enqueued): 8 conserved fields at
+  // the returned pointer, then u_x, u_y, u_z, p (4 fields); valid until the next call
+  virtual const double* stage_real_state() = 0;
+  virtual long long grid_points() const = 0;
+  virtual int variant() const = 0;
 };
 
 // T: compute type of the transforms and products; TS: storage type of the state, the RK
@@ -576,6 +581,18 @@ template <class T, class TS = T> class Engine : public EngineBase {
     enqueue_stage(irk - 1, false, true);
     wait(tmo());
   }
+  const double* stage_real_state() override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    const Geo& g = gfull;
+    inverse3d(B.U, 8);
+    double* out = (double*)B.W2;  // 12 real float64 fields fit in 15 complex fields
+    k_download_convert<TS><<<1024, 256, 0, stream>>>((const SRS*)B.W1, out, out + 8 * g.fsr, g.fsr, P.gamma,
+                                                     P.variant == LAPS_VARIANT_3DI);
+    LAPS_CK(cudaGetLastError());
+    return out;
+  }
+  long long grid_points() const override { return gfull.fsr; }
+  int variant() const override { return P.variant; }
   void download(double* uu, double* prim) override {
     if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
     const Geo& g = gfull;

@@ -539,7 +539,10 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
 #ifndef LAPS_MINB_COL
 #define LAPS_MINB_COL 5
 #endif
-template <class T> struct ColOcc { static constexpr int V = sizeof(typename Store<T>::C) == 8 ? LAPS_MINB_COL : 1; };
+// (float-float: 4 and FP64: 3, the budgets the compiler picks for them without a bound)
+template <class T> struct ColOcc {
+  static constexpr int V = sizeof(typename Store<T>::C) == 8 ? LAPS_MINB_COL : (std::is_same<T, double>::value ? 3 : 4);
+};
 
 // ============================================================================ pass D
 // forward y-FFT of the fluxes with the kx, ky parts of the spectral right-hand side folded

@@ -100,6 +100,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_upload_spectral": (C.c_int, [vp, dp]),
         "laps_diagnostics": (C.c_int, [vp, P(laps_diag)]),
         "laps_spectrum": (C.c_int, [vp, C.c_int, dp, dp]),
+        "laps_write_output": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "laps_read_restart": (C.c_int, [vp, C.c_char_p, dp]),
         "laps_wait": (C.c_int, [vp, C.c_int]),
         "laps_get_time": (C.c_int, [vp, dp, dp]),
         "laps_get_info": (C.c_int, [vp, P(laps_info)]),
@@ -232,6 +234,16 @@ class Laps:
         eb = np.zeros(nshell)
         self._ck(self.lib.laps_spectrum(self.h, int(nshell), _dptr(eu), _dptr(eb)))
         return eu, eb
+
+    def write_output(self, path, primitive: bool = True):
+        """Write the state as the reference's outNNN.dat."""
+        self._ck(self.lib.laps_write_output(self.h, os.fsencode(path), LAYOUT_PRIMITIVE if primitive else LAYOUT_CONSERVED))
+
+    def read_restart(self, path) -> float:
+        """Read an outNNN.dat (primitive), upload it and set the time; returns the time."""
+        t = C.c_double()
+        self._ck(self.lib.laps_read_restart(self.h, os.fsencode(path), C.byref(t)))
+        return t.value
 
     def time(self):
         t, d = C.c_double(), C.c_double()

@@ -175,3 +175,20 @@ def test_shell_spectra_parseval_and_single_mode():
     uu[5] = np.sin(4 * x)[None, :, None]            # |k| = 4, energy 1/4
     _, eb = laps3d.shell_spectra(uu, 2 * np.pi, 2 * np.pi, 2 * np.pi, 8)
     assert np.allclose(eb, [0, 0, 0, 0.25, 0.25, 0, 0, 0], atol=1e-15)
+
+
+def test_output_file_layout(tmp_path):
+    """The restated outNNN.dat: 12-byte time record (markers 4, float32), then float64 data in
+    Fortran order; a read gives back the array and the time rounded to float32."""
+    from oracle import outfile
+
+    rng = np.random.default_rng(3)
+    uu = rng.standard_normal((8, 4, 3, 16))
+    raw = outfile.write_output(tmp_path / outfile.output_name(7), uu, 1.2345678901)
+    assert outfile.output_name(7) == "out007.dat" and outfile.output_name(123) == "out123.dat"
+    assert len(raw) == 12 + 8 * uu.size
+    assert raw[:4] == b"\x04\x00\x00\x00" and raw[8:12] == b"\x04\x00\x00\x00"
+    assert np.frombuffer(raw[12:20], "<f8")[0] == uu[0, 0, 0, 0]   # x fastest
+    assert np.frombuffer(raw[20:28], "<f8")[0] == uu[0, 0, 0, 1]
+    t, back = outfile.read_output(tmp_path / "out007.dat", (16, 3, 4))
+    assert np.array_equal(back, uu) and t == float(np.float32(1.2345678901))
