@@ -6,7 +6,7 @@ module laps_gpu
     implicit none
 
     integer(c_int), parameter :: LAPS_OK = 0
-    integer(c_int), parameter :: LAPS_STATUS_NAN = 1, LAPS_STATUS_DT_FLOOR = 2
+    integer(c_int), parameter :: LAPS_STATUS_NAN = 1, LAPS_STATUS_DT_FLOOR = 2, LAPS_STATUS_DEVICE_TIMEOUT = 4
     integer(c_int), parameter :: LAPS_VARIANT_3DC = 0, LAPS_VARIANT_3DI = 1, LAPS_VARIANT_2DC = 2
     integer(c_int), parameter :: LAPS_PREC_FP64 = 0, LAPS_PREC_DD = 1, LAPS_PREC_FP32 = 2, &
         LAPS_PREC_FP32_F64 = 3

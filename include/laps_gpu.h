@@ -39,6 +39,7 @@ extern "C" {
 /* status bits returned by laps_step / laps_vardt */
 #define LAPS_STATUS_NAN 1       /* a NaN was met in the CFL reduction */
 #define LAPS_STATUS_DT_FLOOR 2  /* dt < 1e-8: step not taken (src_compressible/mhd.f90:216) */
+#define LAPS_STATUS_DEVICE_TIMEOUT 4 /* a bounded device-side wait (tile copy) ran out; results invalid */
 
 /* variants (the reference ships one source tree per variant) */
 #define LAPS_VARIANT_3DC 0 /* 3-D compressible, src_compressible/ */

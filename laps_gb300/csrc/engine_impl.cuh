@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 #include <chrono>
+#include <cudaTypedefs.h>
 #include <thread>
 #include "launch.cuh"
 #include "diag.cuh"
@@ -41,6 +42,35 @@ template <class T> std::vector<typename Store<T>::C> twiddles(int n) {
     t[j] = host_cplx<T>(cosl(a), -sinl(a));
   }
   return t;
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    LAPS_CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw Error{LAPS_ECUDA, "cuTensorMapEncodeTiled is not available"};
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// A work buffer of nfields fields seen by the tile copies: 8-byte elements, dim 0 = kx
+// (kxp * ew elements, ew = complex bytes / 8), dim 1 = y, dim 2 = z + field * nz; box
+// {TX * ew, by, bz}.
+inline CUtensorMap work_tensor_map(void* base, const Geo& g, int nfields, int ew, int by, int bz) {
+  CUtensorMap m;
+  cuuint64_t dims[3] = {(cuuint64_t)g.kxp * ew, (cuuint64_t)g.ny, (cuuint64_t)g.nz * nfields};
+  cuuint64_t strides[2] = {(cuuint64_t)g.kxp * ew * 8, (cuuint64_t)g.ny * g.kxp * ew * 8};
+  cuuint32_t box[3] = {(cuuint32_t)(TX * ew), (cuuint32_t)by, (cuuint32_t)bz};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box, es,
+                                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error{LAPS_ECUDA, "tensor map encoding failed (" + std::to_string((int)r) + ")"};
+  return m;
 }
 
 class EngineBase {
@@ -106,6 +136,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
   StepState* st = nullptr;
   StepState* h_st = nullptr;  // pinned mirror
   double* d_part = nullptr;   // diagnostics partial sums
+  CUtensorMap tm_d{}, tm_e{};  // tile copies of pass D (y columns of W1) and E (z columns of W2)
   int npart = 0;
 
   template <class X> X* dalloc(size_t n) {
@@ -233,6 +264,11 @@ template <class T, class TS = T> class Engine : public EngineBase {
     B.W1 = (C*)dalloc<unsigned char>(19 * g.fsc * WE);
     B.W2 = (C*)dalloc<unsigned char>(w2_fields(q) * g.fsc * WE);
     bytes = plan_bytes(q) - (1 << 20);
+    {
+      const int ew = (int)(sizeof(C) / 8);
+      tm_d = work_tensor_map(B.W1, g, 19, ew, std::min(q.ny, 256), 1);
+      tm_e = work_tensor_map(B.W2, g, w2_fields(q), ew, 1, std::min(q.nz, 256));
+    }
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
     LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
     auto up = [&](auto* dst, const auto& src) {
@@ -375,13 +411,13 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.e_first = 0;
     return a;
   }
-  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz); }
-  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy); }
+  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, nullptr); }
+  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, nullptr); }
   void passC(const PassArgs& a) { launch_passC<T, TS>(stream, p.nx, B, a, passk(), twx); }
-  void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy); }
+  void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passE(const PassArgs& a) {
-    if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T, TS>(stream, p.nz, B, a, passk(), twz);
-    else launch_passE<T, TS>(stream, p.nz, B, a, passk(), twz);
+    if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T, TS>(stream, p.nz, B, a, passk(), twz, nullptr);
+    else launch_passE<T, TS>(stream, p.nz, B, a, passk(), twz, &tm_e);
   }
 
   // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage

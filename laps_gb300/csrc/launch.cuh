@@ -2,6 +2,7 @@
 // is explicitly instantiated per element type in its own translation unit (launch_*.cu)
 // so that the float-float FFT code compiles in parallel.
 #pragma once
+#include <cuda.h>
 #include <string>
 #include "passes.cuh"
 
@@ -37,8 +38,10 @@ void launch_rows_r2c(cudaStream_t stream, int nx, const typename Store<T>::R* in
 template <class T>
 void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in, typename Store<T>::R* out, long long nrows, int kxp,
                      const typename Store<T>::C* twx);
-template <class T, class TS> void launch_passA(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
-template <class T, class TS> void launch_passB(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passA(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
+                                             const CUtensorMap* tm);
+template <class T, class TS> void launch_passB(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
+                                             const CUtensorMap* tm);
 template <class T, class TS, int INCOMP, int CFL>
 void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
 template <class T, class TS>
@@ -51,8 +54,11 @@ void launch_passC(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T
     else launch_passC_v<T, TS, 0, 0>(stream, N, B, a, kk, tw);
   }
 }
-template <class T, class TS> void launch_passD(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
-template <class T, class TS> void launch_passE(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
-template <class T, class TS> void launch_passE3i(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw);
+template <class T, class TS> void launch_passD(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
+                                             const CUtensorMap* tm);
+template <class T, class TS> void launch_passE(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
+                                             const CUtensorMap* tm);
+template <class T, class TS> void launch_passE3i(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
+                                             const CUtensorMap* tm);
 
 }  // namespace laps

@@ -57,7 +57,8 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
 
 #define LAPS_COL_PASS(NAME, KERNEL, NOUTER)                                                                              \
   template <class T, class TS>                                                                                          \
-  void NAME(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw) {  \
+  void NAME(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,   \
+            const CUtensorMap* tm) {                                                                                   \
     switch (N) { LAPS_COL_SIZES(LAPS_CASE) default: throw Error{LAPS_EINVAL, "unsupported line length"}; }               \
     LAPS_CK(cudaGetLastError());                                                                                        \
   }
@@ -88,7 +89,7 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
     using CL = Col<T, NN>;                                                                                              \
     set_smem(k_passD<T, TS, NN>, 2 * CL::SMEM);                                                                             \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : (a.mass_from_state ? 6 : 8)); \
-    k_passD<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw);                                       \
+    k_passD<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw, *tm);                                       \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passD, k_passD, nz)
@@ -105,7 +106,7 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
       a0.e_first = 1;                                                                                                   \
       grid.z = 7;                                                                                                       \
     }                                                                                                                   \
-    k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw);                                     \
+    k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw, *tm);                                     \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passE, k_passE, nky)

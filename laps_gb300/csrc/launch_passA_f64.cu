@@ -1,5 +1,5 @@
 // Pass A launcher (double transforms, double state).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passA<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*);
+template void launch_passA<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*, const CUtensorMap*);
 }  // namespace laps

@@ -1,5 +1,5 @@
 // Pass B launcher (double transforms, double state).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passB<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*);
+template void launch_passB<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*, const CUtensorMap*);
 }  // namespace laps

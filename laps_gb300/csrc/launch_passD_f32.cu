@@ -1,5 +1,5 @@
 // Pass D launcher (float transforms, dd state).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passD<float, dd>(cudaStream_t, int, Bufs<float, dd>, PassArgs, PassK<float, dd>, const Store<float>::C*);
+template void launch_passD<float, dd>(cudaStream_t, int, Bufs<float, dd>, PassArgs, PassK<float, dd>, const Store<float>::C*, const CUtensorMap*);
 }  // namespace laps

@@ -1,5 +1,5 @@
 // Pass E3i launcher (double transforms, double state).
 #include "launch_defs.cuh"
 namespace laps {
-template void launch_passE3i<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*);
+template void launch_passE3i<double, double>(cudaStream_t, int, Bufs<double, double>, PassArgs, PassK<double, double>, const Store<double>::C*, const CUtensorMap*);
 }  // namespace laps

@@ -6,6 +6,7 @@
 #pragma once
 #include <type_traits>
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace laps {
 
@@ -573,14 +574,17 @@ __constant__ DGroup c_dgroups[2][8] = {
      {{5, -1, -1}, DG_EZ, 6}}};
 
 template <class T, class TS, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V) k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
+__global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V)
+    k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy,
+            const __grid_constant__ CUtensorMap tmap) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NY>;
   using C = typename Store<T>::C;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_tma[];  // 128-byte aligned: TMA destinations
+  __shared__ __align__(8) uint64_t tbar[2];
   if (a.st->halt) return;
-  ColCtx<T, NY, 2> x(reinterpret_cast<C*>(smem_raw));
+  ColCtx<T, NY, 2> x(reinterpret_cast<C*>(smem_tma));
   const Geo& g = a.g;
   const DGroup grp = c_dgroups[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][blockIdx.z + (a.mass_from_state ? 2 : 0)];
   int kx = blockIdx.x * TX + x.c;
@@ -592,31 +596,39 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V) k_passD(Buf
   const int kind = grp.kind;
   const int nin = grp.in[1] < 0 ? 1 : (grp.in[2] < 0 || (kind == DG_Q8 && !a.aeb) ? 2 : 3);
   C* ob = b.W2 + col + grp.out * g.fsc;
-  // inputs 0 and 1 are loaded together and transformed together; a third goes into the
-  // buffer its group has finished with
-  auto load = [&](int k, int bi) {
-    const C* in = b.W1 + grp.in[k] * g.fsc + col;
-#pragma unroll
-    for (int m = 0; m < CL::EPT; m++) {
-      cx<T> v = ok ? Store<T>::ldg(in + (long long)x.j(m) * g.kxp) : cx_zero<T>();
-      Store<T>::stc(x.at(bi, m), v);
+  // Input tiles come by TMA (one copy per tile and 256-line box, issued by thread 0): inputs
+  // 0 and 1 at the start into buffers 0 and 1, a third into the buffer its group has finished
+  // with.  FP32 lines transform inputs 0 and 1 together; wider types one after the other.
+  TileLoad tl;
+  tl.init(tbar);
+  auto issue = [&](int k, int bi) {
+    if (threadIdx.x == 0) {
+      constexpr int EW = (int)(sizeof(C) / 8), YB = NY < 256 ? NY : 256;
+      const int z0 = blockIdx.y * CL::NTILE;
+      const int nt = g.nz - z0 < CL::NTILE ? g.nz - z0 : CL::NTILE;
+      tl.expect(bi, (uint32_t)(nt * NY * TX * (int)sizeof(C)));
+      for (int t = 0; t < nt; t++) {
+        C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + bi) * NY * TX;  // tile t, buffer bi
+        for (int y0 = 0; y0 < NY; y0 += YB) tl.copy(bi, dst + y0 * TX, &tmap, blockIdx.x * TX * EW, y0, grp.in[k] * g.nz + z0 + t);
+      }
     }
   };
-  // FP32 lines: inputs 0 and 1 loaded together and transformed together; wider types one
-  // input at a time (register budget)
   constexpr bool PAIR = sizeof(C) == 8;
+  issue(0, 0);
+  if (nin > 1) issue(1, 1);
   if (PAIR) {
-    load(0, 0);
-    if (nin > 1) load(1, 1);
-    __syncthreads();
+    if (!tl.wait(0, a.st) || (nin > 1 && !tl.wait(1, a.st))) return;
     fft_lines_pair<T, NY, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twy, 1);
   }
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
     if (k == 2 || !PAIR) {
       const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
-      load(k, bi);
-      __syncthreads();
+      if (k == 2) {  // the buffer's earlier contents were read and written by the threads
+        if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(2, bi);
+      }
+      if (!tl.wait(bi, a.st)) return;
       fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
     }
     if (ok) {
@@ -752,14 +764,17 @@ __device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& p
 // the time advance of variable v = blockIdx.z.  Tile: kx0..kx0+7, one kept ky row; reads all
 // z of W2, writes kept kz of U (and R).
 template <class T, class TS, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V) k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V)
+    k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz,
+            const __grid_constant__ CUtensorMap tmap) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;
   using C = typename Store<T>::C;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_tma[];  // 128-byte aligned: TMA destinations
+  __shared__ __align__(8) uint64_t tbar[2];
   if (a.st->halt) return;
-  ColCtx<T, NZ, 2> x(reinterpret_cast<C*>(smem_raw));
+  ColCtx<T, NZ, 2> x(reinterpret_cast<C*>(smem_tma));
   const Geo& g = a.g;
   const int v = blockIdx.z + a.e_first;
   int kx = blockIdx.x * TX + x.c;
@@ -774,26 +789,44 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V) k_passE(Buf
   const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
   const int in2 = (v == 6 || a.P.two_d) ? -1 : v == 4 ? 9 : v == 5 ? 8 : v == 7 ? 14 : 2 * v + 1;
   const int nin = in2 < 0 ? 1 : 2;  // (the continuity update from the momentum is k_mass_rk)
-  auto load = [&](int k) {
-    const C* in = b.W2 + (k == 0 ? in1 : in2) * g.fsc + col;
-#pragma unroll
-    for (int m = 0; m < CL::EPT; m++) {
-      cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
-      Store<T>::stc(x.at(k, m), w);
+  // Both input tiles come by TMA, issued at the start by thread 0 (tiles of 128-byte
+  // multiples; a 2-D run's one-point z lines load through the threads instead)
+  constexpr bool TMA = (NZ * TX * (int)sizeof(C)) % 128 == 0;
+  if constexpr (TMA) {
+    TileLoad tl;
+    tl.init(tbar);
+    if (threadIdx.x == 0) {
+      constexpr int EW = (int)(sizeof(C) / 8), ZB = NZ < 256 ? NZ : 256;
+      const int r0 = blockIdx.y * CL::NTILE;
+      const int nt = g.nky() - r0 < CL::NTILE ? g.nky() - r0 : CL::NTILE;
+      for (int k = 0; k < nin; k++) {
+        tl.expect(k, (uint32_t)(nt * NZ * TX * (int)sizeof(C)));
+        const int fin = k == 0 ? in1 : in2;
+        for (int t = 0; t < nt; t++) {
+          C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + k) * NZ * TX;  // tile t, buffer k
+          const int kyt = g.ky_of(r0 + t);
+          for (int z0 = 0; z0 < NZ; z0 += ZB) tl.copy(k, dst + z0 * TX, &tmap, blockIdx.x * TX * EW, kyt, fin * g.nz + z0);
+        }
+      }
     }
-  };
-  if constexpr (sizeof(C) == 8) {  // FP32 lines: both inputs in flight, transformed together
-    load(0);
-    if (nin > 1) load(1);
-    __syncthreads();
-    fft_lines_pair<T, NZ, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twz, 1);
+    if (!tl.wait(0, a.st) || (nin > 1 && !tl.wait(1, a.st))) return;
   } else {
 #pragma unroll 1
     for (int k = 0; k < nin; k++) {
-      load(k);
-      __syncthreads();
-      fft_lines<T, NZ, -1, TX, 1>(x.buf(k), x.c, x.t, true, twz, 1);
+      const C* in = b.W2 + (k == 0 ? in1 : in2) * g.fsc + col;
+#pragma unroll
+      for (int m = 0; m < CL::EPT; m++) {
+        cx<T> w = ok ? Store<T>::ldg(in + x.j(m) * zs) : cx_zero<T>();
+        Store<T>::stc(x.at(k, m), w);
+      }
     }
+    __syncthreads();
+  }
+  if constexpr (sizeof(C) == 8) {  // FP32 lines: the two inputs transformed together
+    fft_lines_pair<T, NZ, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twz, 1);
+  } else {
+    fft_lines<T, NZ, -1, TX, 1>(x.buf(0), x.c, x.t, true, twz, 1);
+    if (nin > 1) fft_lines<T, NZ, -1, TX, 1>(x.buf(1), x.c, x.t, true, twz, 1);
   }
   if (!ok) return;
   using CS = typename Store<TS>::C;

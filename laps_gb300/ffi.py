@@ -24,6 +24,7 @@ LAPS_ETIMEDOUT = -4
 LAPS_ESTATE = -5
 LAPS_STATUS_NAN = 1
 LAPS_STATUS_DT_FLOOR = 2
+LAPS_STATUS_DEVICE_TIMEOUT = 4
 VARIANT_3DC, VARIANT_3DI, VARIANT_2DC = 0, 1, 2
 PREC_FP64, PREC_DD, PREC_FP32, PREC_FP32_F64 = 0, 1, 2, 3
 LAYOUT_PRIMITIVE, LAYOUT_CONSERVED = 0, 1
