@@ -743,6 +743,36 @@ struct RkCtx {
     }
     Store<T>::stc(U, un);
   }
+  // The same update when the right-hand side is an FP32 value (FP32-transform modes): the
+  // expansion / explicit-diffusion terms and the increment cc fnl + ddc r are formed in FP32,
+  // which is the accuracy the right-hand side has; the accumulation u + increment and the
+  // implicit-diffusion factor, which multiply the state itself, stay in the state type.
+  // cf: the FP32 constants (ebm, nu, eta).
+  __device__ __forceinline__ void update_f32(int v, cx<float> fnl, cx<T> u, cx<float> r, typename Store<T>::C* U, CR* R, T k2,
+                                             int kx, int ky, int kz, const PT<float>& cf, float ccf, float ddcf,
+                                             float itf) const {
+    const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
+    const cx<float> uf = cvtc<float>(u);
+    const float k2f = Cvt<float, T>::r(k2);
+    if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - uf * (cf.ebm[v] * itf);
+    if (mom && P->visc && P->visc_exp) fnl = fnl - uf * (cf.nu * k2f);
+    if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - uf * (cf.eta * k2f);
+    cx<float> inc = fnl * ccf;
+    if (stage > 0) inc = fnl * ccf + r * ddcf;
+    if (store_rk) Store<TR>::stc(R, cvtc<TR>(fnl));
+    cx<T> un = u + cvtc<T>(inc);
+    const bool vimp = mom && P->visc && !P->visc_exp, rimp = mag && P->resis && !P->resis_exp;
+    if (vimp || rimp) {
+      const T id = pc->one / (ts * k2 * (vimp ? pc->nu : pc->eta) + pc->one);
+      un = {un.re * id, un.im * id};
+    }
+    if (P->dealias == 1 || P->dealias == 3) {
+      if (kx >= K->kxlim[kz * g->ny + ky]) un = cx_zero<T>();
+    } else if (P->dealias == 2) {
+      un = ((un * K->fx[kx]) * K->fy[ky]) * K->fz[kz];
+    }
+    Store<T>::stc(U, un);
+  }
 };
 
 template <class TR, class T>
@@ -831,6 +861,9 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V)
   if (!ok) return;
   using CS = typename Store<TS>::C;
   const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
+  // FP32 transforms with a wider state: FP32 increments (RkCtx::update_f32)
+  constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
+  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
   const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
   CS* U = b.U + v * g.fsc + col;
   C* R = b.R + v * g.fsc + col;
@@ -862,7 +895,8 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V)
         f = v == 4 ? f + w : f - w;
       }
       TS k2 = need_k2 ? rk.k2(kx, ky, kz) : kk.ps.zero;
-      rk.update(v, cvtc<TS>(f), uo[i], ro[i], U + idx, R + idx, k2, kx, ky, kz);
+      if constexpr (F32INC) rk.update_f32(v, f, uo[i], cvtc<float>(ro[i]), U + idx, R + idx, k2, kx, ky, kz, pc, ccf, ddcf, itf);
+      else rk.update(v, cvtc<TS>(f), uo[i], ro[i], U + idx, R + idx, k2, kx, ky, kz);
     }
   }
 }
