@@ -412,7 +412,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     return a;
   }
   void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, nullptr); }
-  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, nullptr); }
+  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passC(const PassArgs& a) { launch_passC<T, TS>(stream, p.nx, B, a, passk(), twx); }
   void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passE(const PassArgs& a) {

@@ -76,10 +76,10 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passB<T, TS, NN>, CL::SMEM);                                                                                 \
+    set_smem(k_passB<T, TS, NN>, 2 * CL::SMEM);                                                                         \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
-    k_passB<T, TS, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, kk, tw);                                           \
+    k_passB<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw, *tm);                                 \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passB, k_passB, nz)

@@ -124,14 +124,17 @@ __device__ __forceinline__ cx<T> bterm(cx<T> v, int f, T ax, T ay) {
 }
 
 template <class T, class TS, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy) {
+__global__ void __launch_bounds__(Col<T, NY>::THREADS)
+    k_passB(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy,
+            const __grid_constant__ CUtensorMap tmap) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NY>;
   using C = typename Store<T>::C;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_tma[];  // 128-byte aligned: TMA destinations
+  __shared__ __align__(8) uint64_t tbar[2];
   if (a.st->halt) return;
-  ColCtx<T, NY, 1> x(reinterpret_cast<C*>(smem_raw));
+  ColCtx<T, NY, 2> x(reinterpret_cast<C*>(smem_tma));
   const Geo& g = a.g;
   const int f = blockIdx.z;
   const int vt = a.P.variant == LAPS_VARIANT_3DI ? 2 : (a.P.two_d ? 1 : 0);
@@ -143,21 +146,54 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS) k_passB(Bufs<T, TS> b, Pa
   long long col = (long long)z * g.ny * g.kxp + kx;  // + y * kxp
   T rr = Real<T>::from_d(a.st->r_ratio);
   const bool kf = e.f0 > 1 || e.f0 < 0 || e.f1 > 1 || e.f1 < 0;
-#pragma unroll
-  for (int m = 0; m < CL::EPT; m++) {
-    int ky = x.j(m);
-    cx<T> v = cx_zero<T>();
-    if (ok && g.ky_in(ky)) {
-      const long long off = col + (long long)ky * g.kxp;
-      auto ld = [&](int f) {
-        return from_state ? cvtc<T>(Store<TS>::ldg(b.U + off + f * g.fsc)) : Store<T>::ldg(b.W1 + off + f * g.fsc);
-      };
-      T ax = pc.zero, ay = pc.zero, az;
-      if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
-      v = bterm(ld(e.in0), e.f0, ax, ay);
-      if (e.in1 >= 0) v = v + bterm(ld(e.in1), e.f1, ax, ay);
+  if (!from_state) {
+    // 3-D: the input tiles (whole y columns) come by TMA into buffers 0 and 1, then each
+    // thread forms its elements of the output in buffer 0 (zero outside the kept ky rows)
+    TileLoad tl;
+    tl.init(tbar);
+    const int nin = e.in1 >= 0 ? 2 : 1;
+    if (threadIdx.x == 0) {
+      constexpr int EW = (int)(sizeof(C) / 8), YB = NY < 256 ? NY : 256;
+      const int z0 = blockIdx.y * CL::NTILE;
+      const int nt = g.nz - z0 < CL::NTILE ? g.nz - z0 : CL::NTILE;
+      for (int k = 0; k < nin; k++) {
+        tl.expect(k, (uint32_t)(nt * NY * TX * (int)sizeof(C)));
+        for (int t = 0; t < nt; t++) {
+          C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + k) * NY * TX;  // tile t, buffer k
+          for (int y0 = 0; y0 < NY; y0 += YB)
+            tl.copy(k, dst + y0 * TX, &tmap, blockIdx.x * TX * EW, y0, (k == 0 ? e.in0 : e.in1) * g.nz + z0 + t);
+        }
+      }
     }
-    Store<T>::stc(x.at(0, m), v);
+    if (!tl.wait(0, a.st) || (nin > 1 && !tl.wait(1, a.st))) return;
+#pragma unroll
+    for (int m = 0; m < CL::EPT; m++) {
+      int ky = x.j(m);
+      cx<T> v = cx_zero<T>();
+      if (ok && g.ky_in(ky)) {
+        T ax = pc.zero, ay = pc.zero, az;
+        if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+        v = bterm(Store<T>::ldc(x.at(0, m)), e.f0, ax, ay);
+        if (nin > 1) v = v + bterm(Store<T>::ldc(x.at(1, m)), e.f1, ax, ay);
+      }
+      Store<T>::stc(x.at(0, m), v);
+    }
+  } else {
+    // 2-D: the state itself (the state type) through the threads
+#pragma unroll
+    for (int m = 0; m < CL::EPT; m++) {
+      int ky = x.j(m);
+      cx<T> v = cx_zero<T>();
+      if (ok && g.ky_in(ky)) {
+        const long long off = col + (long long)ky * g.kxp;
+        auto ld = [&](int fi) { return cvtc<T>(Store<TS>::ldg(b.U + off + fi * g.fsc)); };
+        T ax = pc.zero, ay = pc.zero, az;
+        if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+        v = bterm(ld(e.in0), e.f0, ax, ay);
+        if (e.in1 >= 0) v = v + bterm(ld(e.in1), e.f1, ax, ay);
+      }
+      Store<T>::stc(x.at(0, m), v);
+    }
   }
   __syncthreads();
   fft_lines<T, NY, +1, TX, 1>(x.buf(0), x.c, x.t, true, twy, 1);
