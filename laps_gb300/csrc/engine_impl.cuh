@@ -137,6 +137,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
   StepState* h_st = nullptr;  // pinned mirror
   double* d_part = nullptr;   // diagnostics partial sums
   CUtensorMap tm_d{}, tm_e{};  // tile copies of pass D (y columns of W1) and E (z columns of W2)
+  CUtensorMap tm_a{};          // pass A: z columns of the state U
   int npart = 0;
 
   template <class X> X* dalloc(size_t n) {
@@ -268,6 +269,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
       const int ew = (int)(sizeof(C) / 8);
       tm_d = work_tensor_map(B.W1, g, 19, ew, std::min(q.ny, 256), 1);
       tm_e = work_tensor_map(B.W2, g, w2_fields(q), ew, 1, std::min(q.nz, 256));
+      tm_a = work_tensor_map(B.U, g, 8, (int)(sizeof(CS) / 8), 1, std::min(q.nz, 256));
     }
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
     LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
@@ -411,7 +413,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.e_first = 0;
     return a;
   }
-  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, nullptr); }
+  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, &tm_a); }
   void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passC(const PassArgs& a) { launch_passC<T, TS>(stream, p.nx, B, a, passk(), twx); }
   void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }

@@ -24,8 +24,10 @@ struct Error {
 #define LAPS_COL_SIZES(X) X(1) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
 #define LAPS_ROW_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
 
+// opt in to more than the default 48 KB per block; the default covers static and dynamic shared
+// memory together, so requests close to it opt in too (kernels keep < 8 KB static)
 template <class K> inline void set_smem(K kernel, int bytes) {
-  if (bytes > 48 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  if (bytes > 40 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
 

@@ -65,10 +65,12 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passA<T, TS, NN>, CL::SMEM);                                                                                 \
+    /* transform tiles, then the state tiles they are formed from */                                                 \
+    const int sm = CL::SMEM + CL::NTILE * NN * TX * (int)sizeof(typename Store<TS>::C);                                 \
+    set_smem(k_passA<T, TS, NN>, sm);                                                                                   \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE,                                     \
               a.P.variant == LAPS_VARIANT_3DI ? 12 : (a.hall ? 10 : 8));                                                \
-    k_passA<T, TS, NN><<<grid, CL::THREADS, CL::SMEM, stream>>>(B, a, kk, tw);                                           \
+    k_passA<T, TS, NN><<<grid, CL::THREADS, sm, stream>>>(B, a, kk, tw, *tm);                                           \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passA, k_passA, nky)

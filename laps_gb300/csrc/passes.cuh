@@ -54,14 +54,20 @@ __constant__ ATab c_atab[2][12] = {
     {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {5, -1}, {4, 1}, {1, 1}, {2, 1}, {3, 1}}};
 
 template <class T, class TS, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz) {
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS)
+    k_passA(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz,
+            const __grid_constant__ CUtensorMap tmap) {
   const PT<T>& pc = kk.pc;
   const KTab<T>& K = kk.K;
   using CL = Col<T, NZ>;
   using C = typename Store<T>::C;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using CS = typename Store<TS>::C;
+  extern __shared__ __align__(128) unsigned char smem_tma[];  // 128-byte aligned: TMA destinations
+  __shared__ __align__(8) uint64_t tbar[2];
   if (a.st->halt) return;
-  ColCtx<T, NZ, 1> x(reinterpret_cast<C*>(smem_raw));
+  ColCtx<T, NZ, 1> x(reinterpret_cast<C*>(smem_tma));
+  // the state tiles (whole z columns, state type) after the NTILE transform tiles
+  CS* raw = reinterpret_cast<CS*>(smem_tma + CL::NTILE * NZ * TX * (int)sizeof(C)) + x.tl * NZ * TX;
   const Geo& g = a.g;
   const int f = blockIdx.z;
   const ATab e = c_atab[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][f];
@@ -71,13 +77,27 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passA(Bufs<T, TS> b, Pa
   int ky = ok ? g.ky_of(r) : 0;
   long long col = (long long)ky * g.kxp + kx;  // + z * ny * kxp
   long long zs = (long long)g.ny * g.kxp;
-  const typename Store<TS>::C* in = b.U + e.src * g.fsc + col;
+  {
+    TileLoad tl;
+    tl.init(tbar);
+    if (threadIdx.x == 0) {
+      constexpr int EW = (int)(sizeof(CS) / 8), ZB = NZ < 256 ? NZ : 256;
+      const int r0 = blockIdx.y * CL::NTILE;
+      const int nt = g.nky() - r0 < CL::NTILE ? g.nky() - r0 : CL::NTILE;
+      tl.expect(0, (uint32_t)(nt * NZ * TX * (int)sizeof(CS)));
+      for (int t = 0; t < nt; t++) {
+        CS* dst = reinterpret_cast<CS*>(smem_tma + CL::NTILE * NZ * TX * (int)sizeof(C)) + t * NZ * TX;
+        for (int z0 = 0; z0 < NZ; z0 += ZB) tl.copy(0, dst + z0 * TX, &tmap, blockIdx.x * TX * EW, g.ky_of(r0 + t), e.src * g.nz + z0);
+      }
+    }
+    if (!tl.wait(0, a.st)) return;
+  }
 #pragma unroll
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.kz_in(kz)) {
-      v = cvtc<T>(Store<TS>::ldg(in + kz * zs));
+      v = cvtc<T>(Store<TS>::ldc(raw + kz * TX + x.c));
       if (e.mult < 0) v = -mul_i(v, K.kzd[kz]);
       else if (e.mult > 0) v = mul_i(v, K.kzd[kz]);
     }
