@@ -330,7 +330,45 @@ struct Flux {
     T dtz = M::div(c.dz, cmax[2]) * rfac;
     return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
   }
+  // The FP32 screen of the CFL bound: the same speeds, with the maximum over
+  // |u +- c_f|, |u +- c_s|, |u +- c_A,d|, |u| written as |u| + c_f (c_f >= c_s and
+  // c_f >= |c_A,d|, so the two agree up to rounding); approximate divide and square root.
+  __device__ __forceinline__ static float cfl_screen(const float* q, const PT<float>& c, const Phys& P, float rfac) {
+    using M = MathFastF;
+    const float rho = q[0], rinv = M::div(1.f, rho);
+    const float ux = q[1] * rinv, uy = q[2] * rinv, uz = q[3] * rinv;
+    const float Bx = q[4], By = q[5], Bz = q[6];
+    const float p = (q[7] - 0.5f * (q[1] * ux + q[2] * uy + q[3] * uz + Bx * Bx + By * By + Bz * Bz)) * c.gm1;
+    const float cs2 = c.gamma * p * rinv;
+    const float b2r = (Bx * Bx + By * By + Bz * Bz) * rinv;  // c_A^2
+    const float cms2 = cs2 + b2r;
+    const float u[3] = {ux, uy, uz};
+    const float ca2[3] = {Bx * Bx * rinv, By * By * rinv, Bz * Bz * rinv};
+    float cmax[3];
+    const int nd = P.two_d ? 2 : 3;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      if (d >= nd) { cmax[d] = 1.f; continue; }
+      const float cns = M::sqrt(fmaxf(cms2 * cms2 - 4.f * cs2 * ca2[d], 0.f));
+      cmax[d] = fabsf(u[d]) + M::sqrt(0.5f * (cms2 + cns));
+    }
+    if (P.two_d && P.resis && P.resis_exp) {
+      cmax[0] = fmaxf(cmax[0], c.eta_dx);
+      cmax[1] = fmaxf(cmax[1], c.eta_dy);
+    }
+    if (P.hall) {
+      const float ch = c.di * rinv * fmaxf(fmaxf(Bx, By), Bz) * c.inv_mindx;
+#pragma unroll
+      for (int d = 0; d < 3; d++) cmax[d] = fmaxf(cmax[d], ch);
+    }
+    float dtx = M::div(c.dx, cmax[0]);
+    if (P.zrad) dtx = dtx * rfac;
+    const float dty = M::div(c.dy, cmax[1]) * rfac;
+    if (P.two_d) return fminf(dtx, dty);
+    return fminf(fminf(dtx, dty), M::div(c.dz, cmax[2]) * rfac);
+  }
 };
+
 
 template <class T>
 struct FluxI {
@@ -385,6 +423,20 @@ struct FluxI {
     T dtz = M::div(c.dz, cmax[2]) * rfac;
     return Real<T>::min_(Real<T>::min_(dtx, dty), dtz);
   }
+  // FP32 screen: max(|u +- c_A,d|, |u|) = |u| + |c_A,d|; approximate divide and square root
+  __device__ __forceinline__ static float cfl_screen(const float* q, const PT<float>& c, const Phys& P, float rfac) {
+    using M = MathFastF;
+    const float rho = q[0], rinv = M::div(1.f, rho), sq = M::sqrt(rho);
+    float cmax[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) cmax[d] = fabsf(q[1 + d] * rinv) + fabsf(M::div(q[4 + d], sq));
+    if (P.hall) {
+      const float ch = c.di * rinv * fmaxf(fmaxf(q[4], q[5]), q[6]) * c.inv_mindx;
+#pragma unroll
+      for (int d = 0; d < 3; d++) cmax[d] = fmaxf(cmax[d], ch);
+    }
+    return fminf(fminf(M::div(c.dx, cmax[0]), M::div(c.dy, cmax[1]) * rfac), M::div(c.dz, cmax[2]) * rfac);
+  }
 };
 
 // pass C transform lists (flux slot numbers): compressible, compressible with the continuity
@@ -433,7 +485,6 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   using CF = PassCCfg<NX, (int)sizeof(C)>;
   using SR = typename Store<T>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[32];
   if (a.st->halt) return;
   C* sc = reinterpret_cast<C*>(smem_raw);  // [row][field] lines of LC complex
   SR* sr = reinterpret_cast<SR*>(smem_raw);
@@ -489,8 +540,8 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   constexpr int NQ = INCOMP ? 19 : 11;
   using PH = typename std::conditional<INCOMP, FluxI<T>, Flux<T>>::type;
   // ---- CFL minimum (vardt, mhd.f90:328-429), screened: every point in FP32 with the
-  // approximate divide and square root, then only the points within 0.1 % of the block's FP32
-  // minimum (or FP32 NaN) in the state type TS.  The screened value of a point's bound is
+  // approximate divide and square root, then only the points within 0.01 % of the block's
+  // FP32 minimum (or FP32 NaN) in the state type TS.  The screened value of a point's bound is
   // within 1e-5 of its TS value, so the block's TS minimum is the one a full TS evaluation
   // gives.
   if (CFL) {
@@ -512,38 +563,74 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
         float qf[NQ];
 #pragma unroll
         for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + f * CF::FSTR)) : 0.f;
-        d32[i] = PHF::template cfl<MathFastF>(qf, pf, a.P, rfac_f);
+        d32[i] = PHF::cfl_screen(qf, pf, a.P, rfac_f);
         m32 = fminf(m32, d32[i]);
       }
     }
+    // candidates: the points within 0.01 % of the block's FP32 minimum, and FP32 NaNs; their
+    // inputs are copied to a list that one warp evaluates in TS while the others go on
+    constexpr int MAXC = 32;
+    __shared__ SR cand[MAXC][NQ];
+    __shared__ int ncand;
+    if (threadIdx.x == 0) ncand = 0;
     for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
     if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = m32;
     __syncthreads();
     for (int w = 0; w < CF::THREADS / 32; w++) m32 = fminf(m32, red32[w]);
-    const float thr = m32 * 1.001f;
-    TS tmin = Real<TS>::inf();
-    bool nan_seen = false;
-#pragma unroll 1
+    const float thr = m32 * 1.0001f;
+#pragma unroll
     for (int i = 0; i < PPT; i++) {
       const int p = threadIdx.x + i * CF::THREADS;
       if (p >= CF::ROWS * NX || (!(d32[i] <= thr) && !isnan(d32[i]))) continue;
-      const SR* base = point_base(p);
-      TS qs[NQ];
+      const int slot = atomicAdd(&ncand, 1);
+      if (slot < MAXC) {
+        const SR* base = point_base(p);
 #pragma unroll
-      for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(base + f * CF::FSTR)) : kk.ps.zero;
-      const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
-      if (Real<TS>::isnan_(d)) nan_seen = true;
-      else tmin = Real<TS>::min_(tmin, d);
+        for (int f = 0; f < NQ; f++) cand[slot][f] = f < nin ? base[f * CF::FSTR] : SR{};
+      }
     }
-    double dmin = Real<TS>::to_d(tmin);
-    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmin;
-    if (__any_sync(0xffffffffu, nan_seen) && (threadIdx.x & 31) == 0) atomicOr(&a.st->status, LAPS_STATUS_NAN);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double m = red[0];
-      for (int w = 1; w < CF::THREADS / 32; w++) m = fmin(m, red[w]);
-      atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(m));
+    __syncthreads();  // the list is complete; the physics may now overwrite the inputs
+    const int nc = ncand;
+    auto report = [&](TS tmin, bool nan_seen) {  // warp min, then one atomic per warp
+      double dmin = Real<TS>::to_d(tmin);
+      for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+      const bool any_nan = __any_sync(0xffffffffu, nan_seen);
+      if ((threadIdx.x & 31) == 0) {
+        if (any_nan) atomicOr(&a.st->status, LAPS_STATUS_NAN);
+        atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(dmin));
+      }
+    };
+    if (nc <= MAXC) {
+      if (threadIdx.x < 32) {
+        TS tmin = Real<TS>::inf();
+        bool nan_seen = false;
+        if ((int)threadIdx.x < nc) {
+          TS qs[NQ];
+#pragma unroll
+          for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(&cand[threadIdx.x][f])) : kk.ps.zero;
+          const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
+          if (Real<TS>::isnan_(d)) nan_seen = true;
+          else tmin = d;
+        }
+        report(tmin, nan_seen);
+      }
+    } else {  // more candidates than the list holds: every thread evaluates its own
+      TS tmin = Real<TS>::inf();
+      bool nan_seen = false;
+#pragma unroll 1
+      for (int i = 0; i < PPT; i++) {
+        const int p = threadIdx.x + i * CF::THREADS;
+        if (p >= CF::ROWS * NX || (!(d32[i] <= thr) && !isnan(d32[i]))) continue;
+        const SR* base = point_base(p);
+        TS qs[NQ];
+#pragma unroll
+        for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(base + f * CF::FSTR)) : kk.ps.zero;
+        const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
+        if (Real<TS>::isnan_(d)) nan_seen = true;
+        else tmin = Real<TS>::min_(tmin, d);
+      }
+      report(tmin, nan_seen);
+      __syncthreads();  // before the physics overwrites the inputs
     }
   }
   if (nfl == 0) return;
