@@ -185,6 +185,28 @@ int laps_diagnostics(laps_ctx* ctx, laps_diag* d);
  * binning of its own.  Either array may be NULL. */
 int laps_spectrum(laps_ctx* ctx, int nshell, double* e_u, double* e_b);
 
+/* Granular entry points in the reference's order, for bisection against its subroutines
+ * (unfused: they recompute what laps_step fuses).  Compressible variants for the flux / rhs
+ * calls (LAPS_EINVAL for the incompressible one).
+ *   laps_calc_flux: calc_flux (mhdrhs.f90:21-124) of the current state, 18 real fields
+ *     flux(nx,ny,nz,1:18) in the reference's order, then the expansion term (:157-171) as
+ *     field 19 when the expanding box is on.
+ *   laps_transform_flux: the same fields forward-transformed (transform_flux_real_to_fourier,
+ *     :128-172), (nx/2+1,ny,nz) interleaved complex each.
+ *   laps_calc_rhs: fnl(nx/2+1,ny,nz,8) of calc_rhs (:174-279, with the expansion and
+ *     explicit-diffusion terms, before rkt); the state is unchanged, the RK register is
+ *     overwritten (call between steps).
+ *   laps_dealias: dealias (dealiasing.f90:70-113) applied to the state.
+ *   laps_transform_uu_k2r / laps_update_prim: transform_uu_fourier_to_real (fftw.f90:73-103)
+ *     and update_uu_prim_from_uu (mhdrhs.f90:282-294): uu(nx,ny,nz,8) / uu_prim(nx,ny,nz,4).
+ * laps_rk_stage is rkt(irk) with the stage's right-hand side; laps_vardt is vardt. */
+int laps_calc_flux(laps_ctx* ctx, double* flux);
+int laps_transform_flux(laps_ctx* ctx, double* flux_fourier);
+int laps_calc_rhs(laps_ctx* ctx, double* fnl);
+int laps_dealias(laps_ctx* ctx);
+int laps_transform_uu_k2r(laps_ctx* ctx, double* uu);
+int laps_update_prim(laps_ctx* ctx, double* uu_prim);
+
 /* The reference's output / restart file outNNN.dat (mhdoutput.f90:72-131, restart.f90:17-63):
  * a Fortran unformatted record with the time as a 4-byte real (12 bytes with its markers),
  * then uu(nx,ny,nz,8) as 8-byte reals in Fortran order.  laps_write_output writes the current

@@ -161,6 +161,27 @@ int laps_spectrum(laps_ctx* c, int nshell, double* e_u, double* e_b) {
   if (!e_u && !e_b) return fail(c, LAPS_EINVAL, "null spectrum arrays");
   return guarded(c, [&] { c->e->spectrum(nshell, e_u, e_b); });
 }
+int laps_calc_flux(laps_ctx* c, double* flux) {
+  if (!flux) return fail(c, LAPS_EINVAL, "null output");
+  return guarded(c, [&] { c->e->calc_flux(flux, 0); });
+}
+int laps_transform_flux(laps_ctx* c, double* flux_fourier) {
+  if (!flux_fourier) return fail(c, LAPS_EINVAL, "null output");
+  return guarded(c, [&] { c->e->calc_flux(flux_fourier, 1); });
+}
+int laps_calc_rhs(laps_ctx* c, double* fnl) {
+  if (!fnl) return fail(c, LAPS_EINVAL, "null output");
+  return guarded(c, [&] { c->e->calc_rhs(fnl); });
+}
+int laps_dealias(laps_ctx* c) { return guarded(c, [&] { c->e->dealias_state(); }); }
+int laps_transform_uu_k2r(laps_ctx* c, double* uu) {
+  if (!uu) return fail(c, LAPS_EINVAL, "null output");
+  return guarded(c, [&] { c->e->download(uu, nullptr); });
+}
+int laps_update_prim(laps_ctx* c, double* uu_prim) {
+  if (!uu_prim) return fail(c, LAPS_EINVAL, "null output");
+  return guarded(c, [&] { c->e->download(nullptr, uu_prim); });
+}
 int laps_wait(laps_ctx* c, int timeout_ms) { return guarded(c, [&] { c->e->wait(timeout_ms); }); }
 int laps_get_time(laps_ctx* c, double* t, double* dt) { return guarded(c, [&] { c->e->get_time(t, dt); }); }
 int laps_get_info(laps_ctx* c, laps_info* i) {

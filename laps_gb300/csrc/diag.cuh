@@ -4,6 +4,7 @@
 // partials in block order, so repeated calls give bitwise-identical results.
 #pragma once
 #include "kernels.cuh"
+#include "passes.cuh"
 
 namespace laps {
 
@@ -229,6 +230,68 @@ __global__ void __launch_bounds__(SPEC_WARPS * 32) k_shell_spectrum(const typena
     double acc = 0.0;
     for (int w = 0; w < SPEC_WARPS; w++) acc += sh[w * 2 * nshell + s];
     part[(size_t)blockIdx.x * 2 * nshell + s] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------- granular path
+// One component of J = i k x B (calc_current_density_real, mhdrhs.f90:296-362, with the
+// expanding-box / corotation factors of kfac), written with the spectral pitch.
+template <class T>
+__global__ void k_spec_curl(const typename Store<T>::C* __restrict__ U, typename Store<T>::C* __restrict__ out, Geo g, KTab<T> K,
+                            Phys P, PT<T> pc, const StepState* st, int comp) {
+  const long long tot = (long long)g.nz * g.ny * g.kxp;
+  const T rr = Real<T>::from_d(st->r_ratio);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % g.kxp);
+    const long long r = i / g.kxp;
+    const int ky = (int)(r % g.ny), kz = (int)(r / g.ny);
+    cx<T> v = cx_zero<T>();
+    if (kx < g.nh) {
+      T ax, ay, az;
+      kfac(K, P, pc, rr, kx, ky, kz, ax, ay, az);
+      const cx<T> bx = Store<T>::ldc(U + 4 * g.fsc + i), by = Store<T>::ldc(U + 5 * g.fsc + i), bz = Store<T>::ldc(U + 6 * g.fsc + i);
+      if (comp == 0) v = mul_i(bz, ay) - mul_i(by, az);
+      else if (comp == 1) v = mul_i(bx, az) - mul_i(bz, ax);
+      else v = mul_i(by, ax) - mul_i(bx, ay);
+    }
+    Store<T>::stc(out + i, v);
+  }
+}
+
+// Flux k of calc_flux (mhdrhs.f90:21-124; k = 18: the expansion term of :157-171) at every
+// point from the real inputs (state, then J), as float64 or in the state type.
+template <class T, bool TO_DOUBLE>
+__global__ void k_flux_point(const typename Store<T>::R* __restrict__ in, long long n, int nin, int k, void* out, PT<T> c,
+                             Phys P, double inv_tau) {
+  const T it = Real<T>::from_d(inv_tau), one = c.one;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T q[11];
+#pragma unroll
+    for (int f = 0; f < 11; f++) q[f] = f < nin ? Store<T>::ld(in + f * n + i) : c.zero;
+    Flux<T>::eval(q, [&](int kk, T v) {
+      if (kk != k) return;
+      if constexpr (TO_DOUBLE) static_cast<double*>(out)[i] = Real<T>::to_d(v);
+      else Store<T>::st(static_cast<typename Store<T>::R*>(out) + i, v);
+    }, c, P, it, one);
+  }
+}
+
+// the dealias mask or filter applied to the state (dealiasing.f90:70-113)
+template <class T>
+__global__ void k_dealias_state(typename Store<T>::C* __restrict__ U, Geo g, KTab<T> K, Phys P) {
+  const long long tot = 8LL * g.fsc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % g.kxp);
+    const long long r = (i / g.kxp) % ((long long)g.ny * g.nz);
+    const int ky = (int)(r % g.ny), kz = (int)(r / g.ny);
+    if (kx >= g.nh) continue;
+    cx<T> v = Store<T>::ldc(U + i);
+    if (P.dealias == 1 || P.dealias == 3) {
+      if (kx >= K.kxlim[kz * g.ny + ky]) v = cx_zero<T>();
+    } else if (P.dealias == 2) {
+      v = ((v * K.fx[kx]) * K.fy[ky]) * K.fz[kz];
+    }
+    Store<T>::stc(U + i, v);
   }
 }
 

@@ -102,6 +102,10 @@ class EngineBase {
   virtual const double* stage_real_state() = 0;
   virtual long long grid_points() const = 0;
   virtual int variant() const = 0;
+  // granular, unfused path (bisection against the reference's subroutines)
+  virtual void calc_flux(double* host, int spectral) = 0;
+  virtual void calc_rhs(double* host) = 0;
+  virtual void dealias_state() = 0;
 };
 
 // T: compute type of the transforms and products; TS: storage type of the state, the RK
@@ -411,6 +415,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.g = g; a.P = P; a.hall = P.hall; a.aeb = P.aeb; a.stage = stage; a.store_rk = store_rk; a.cfl = cfl; a.st = st;
     a.mass_from_state = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
     a.e_first = 0;
+    a.rhs_only = rhs_mode;
     return a;
   }
   void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, &tm_a); }
@@ -423,8 +428,10 @@ template <class T, class TS = T> class Engine : public EngineBase {
   }
 
   // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage
-  const Geo& g_in() const { return (prune_ok && dealiased) ? gprune : gfull; }
-  const Geo& g_out() const { return prune_ok ? gprune : gfull; }
+  const Geo& g_in() const { return (prune_ok && dealiased && !force_full) ? gprune : gfull; }
+  const Geo& g_out() const { return (prune_ok && !force_full) ? gprune : gfull; }
+  bool rhs_mode = false;    // pass E stores fnl in R and leaves the state (calc_rhs)
+  bool force_full = false;  // every pass over the whole spectrum (calc_rhs)
 
   // one stage: stage = 0..2; cfl: compute the CFL minimum and finalise dt before D
   void enqueue_stage(int stage, bool cfl, bool store_rk) {
@@ -663,6 +670,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
   }
   void diagnostics(laps_diag* d) override;
   void spectrum(int nshell, double* eu, double* eb) override;
+  void calc_flux(double* host, int spectral) override;
+  void calc_rhs(double* host) override;
+  void dealias_state() override;
   double* d_spec = nullptr;  // per-block shell partials of spectrum()
   size_t spec_cap = 0;
   void get_time(double* t, double* dt) override {
@@ -682,6 +692,92 @@ template <class T, class TS = T> class Engine : public EngineBase {
     i->graph = graph_steady != nullptr;
   }
 };
+
+// ---------------------------------------------------------------------------- granular path
+// calc_flux (mhdrhs.f90:21-124) alone: the state and, with the Hall term, J = i k x B
+// (calc_current_density_real, :296-362) to real space, then the fluxes one at a time, as real
+// fields or (spectral != 0) forward-transformed like transform_flux_real_to_fourier
+// (:128-172).  Output: nflux fields of nx*ny*nz reals, or of (nx/2+1)*ny*nz complex values.
+template <class T, class TS> void Engine<T, TS>::calc_flux(double* host, int spectral) {
+  if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+  if (P.variant == LAPS_VARIANT_3DI) throw Error{LAPS_EINVAL, "the flux entry points serve the compressible variants"};
+  const Geo& g = gfull;
+  read_state();
+  const long long n = g.fsr;
+  const int nb = 1024;
+  SRS* real = (SRS*)B.W1;  // inputs: state 0..7, J 8..10
+  inverse3d(B.U, 8);
+  CS* w2 = W2s();
+  const long long w2f = w2_fields(p) * WE / (long long)sizeof(CS);  // W2 capacity in CS fields
+  CS* slot = w2 + (w2f - 1) * g.fsc;
+  int nin = 8;
+  if (P.hall) {
+    for (int c = 0; c < 3; c++) {
+      k_spec_curl<TS><<<nb, 256, 0, stream>>>(B.U, slot, g, ktab_s(), P, ps, st, c);
+      LAPS_CK(cudaGetLastError());
+      // one field: z then y columns in W2 field 0, then the rows into the input slot
+      col_plain(slot, w2, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twzs);
+      col_plain(w2, w2, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twys);
+      rows_c2r(w2, real + (8 + c) * n, (long long)g.ny * g.nz);
+    }
+    nin = 11;
+  }
+  const int nflux = 18 + (P.aeb ? 1 : 0);
+  const long long nspec = (long long)g.nz * g.ny * g.nh;
+  for (int k = 0; k < nflux; k++) {
+    if (!spectral) {
+      double* out = (double*)(w2 + 4 * g.fsc);  // n doubles fit in one 16-byte complex field
+      k_flux_point<TS, true><<<nb, 256, 0, stream>>>(real, n, nin, k, out, ps, P, h_st->inv_tau);
+      LAPS_CK(cudaGetLastError());
+      LAPS_CK(cudaMemcpyAsync(host + k * n, out, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    } else {
+      SRS* fr = (SRS*)(w2 + 4 * g.fsc);  // the flux field (state-type reals)
+      k_flux_point<TS, false><<<nb, 256, 0, stream>>>(real, n, nin, k, fr, ps, P, h_st->inv_tau);
+      LAPS_CK(cudaGetLastError());
+      forward3d(fr, slot, 1);  // W2 field 0 as scratch
+      double2* ref = (double2*)(w2 + 8 * g.fsc);
+      k_spec_to_ref<TS><<<nb, 256, 0, stream>>>(slot, ref, g, 1);
+      LAPS_CK(cudaGetLastError());
+      LAPS_CK(cudaMemcpyAsync(host + 2 * k * nspec, ref, nspec * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    }
+    wait(tmo());
+  }
+}
+
+// calc_rhs (mhdrhs.f90:174-279) alone: the fused passes over the whole spectrum with pass E
+// storing fnl (with the expansion and explicit-diffusion terms, before rkt) in R; the state
+// is left as it was.  Overwrites the RK register, so it belongs between steps.
+template <class T, class TS> void Engine<T, TS>::calc_rhs(double* host) {
+  if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+  if (P.variant == LAPS_VARIANT_3DI) throw Error{LAPS_EINVAL, "laps_calc_rhs serves the compressible variants"};
+  const Geo& g = gfull;
+  const bool was = dealiased;
+  rhs_mode = true;
+  force_full = true;
+  try {
+    LAPS_CK(cudaMemsetAsync(&st->halt, 0, sizeof(int), stream));
+    enqueue_stage(0, false, true);
+  } catch (...) {
+    rhs_mode = force_full = false;
+    dealiased = was;
+    throw;
+  }
+  rhs_mode = force_full = false;
+  dealiased = was;
+  double2* ref = (double2*)B.W1;
+  k_spec_to_ref<T><<<1024, 256, 0, stream>>>(B.R, ref, g, 8);
+  LAPS_CK(cudaGetLastError());
+  LAPS_CK(cudaMemcpyAsync(host, ref, (size_t)8 * g.nz * g.ny * g.nh * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+  wait(tmo());
+}
+
+// dealias (dealiasing.f90:70-113) applied to the state
+template <class T, class TS> void Engine<T, TS>::dealias_state() {
+  if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+  k_dealias_state<TS><<<1024, 256, 0, stream>>>(B.U, gfull, ktab_s(), P);
+  LAPS_CK(cudaGetLastError());
+  wait(tmo());
+}
 
 // ---------------------------------------------------------------------------- diagnostics
 template <class T, class TS> void Engine<T, TS>::spectrum(int nshell, double* eu, double* eb) {

@@ -22,6 +22,7 @@ struct PassArgs {
                         // in pass E and passes C, D skip fluxes 1..3
   int e_first;     // pass E: variable of blockIdx.z = 0 (the continuity update runs in a launch
                    // of its own before the momentum is overwritten)
+  int rhs_only;    // store the right-hand side (fnl) in R and leave the state (laps_calc_rhs)
   StepState* st;
 };
 
@@ -847,7 +848,7 @@ struct RkCtx {
   const PT<T>* pc;
   const KTab<T>* K;
   T cc, ddc, ts, inv_tau, rr;
-  int stage, store_rk, plain;
+  int stage, store_rk, plain, rhs_only;
   __device__ __forceinline__ T k2(int kx, int ky, int kz) const {
     if (P->corot && !plain) return ksq(*K, *P, *pc, rr, kx, ky, kz);
     return (K->kx2[kx] + K->ky2[ky]) + K->kz2[kz];
@@ -868,6 +869,10 @@ struct RkCtx {
     if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - u * (pc->ebm[v] * inv_tau);
     if (mom && P->visc && P->visc_exp) fnl = fnl - u * (pc->nu * k2);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - u * (pc->eta * k2);
+    if (rhs_only) {  // calc_rhs alone: fnl with the expansion and explicit-diffusion terms
+      Store<TR>::stc(R, cvtc<TR>(fnl));
+      return;
+    }
     cx<T> un = fnl * cc + u;
     if (stage > 0) un = (fnl * cc + r * ddc) + u;
     if (store_rk) Store<TR>::stc(R, cvtc<TR>(fnl));
@@ -900,6 +905,10 @@ struct RkCtx {
     if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - uf * (cf.ebm[v] * itf);
     if (mom && P->visc && P->visc_exp) fnl = fnl - uf * (cf.nu * k2f);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - uf * (cf.eta * k2f);
+    if (rhs_only) {
+      Store<TR>::stc(R, cvtc<TR>(fnl));
+      return;
+    }
     cx<float> inc = fnl * ccf;
     if (stage > 0) inc = fnl * ccf + r * ddcf;
     if (store_rk) Store<TR>::stc(R, cvtc<TR>(fnl));
@@ -930,6 +939,7 @@ __device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& p
   r.inv_tau = Real<T>::from_d(a.st->inv_tau);
   r.rr = Real<T>::from_d(a.st->r_ratio);
   r.plain = a.st->ksq_plain;
+  r.rhs_only = a.rhs_only;
   return r;
 }
 

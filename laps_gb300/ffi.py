@@ -102,6 +102,12 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_diagnostics": (C.c_int, [vp, P(laps_diag)]),
         "laps_spectrum": (C.c_int, [vp, C.c_int, dp, dp]),
         "laps_write_output": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "laps_calc_flux": (C.c_int, [vp, dp]),
+        "laps_transform_flux": (C.c_int, [vp, dp]),
+        "laps_calc_rhs": (C.c_int, [vp, dp]),
+        "laps_dealias": (C.c_int, [vp]),
+        "laps_transform_uu_k2r": (C.c_int, [vp, dp]),
+        "laps_update_prim": (C.c_int, [vp, dp]),
         "laps_read_restart": (C.c_int, [vp, C.c_char_p, dp]),
         "laps_wait": (C.c_int, [vp, C.c_int]),
         "laps_get_time": (C.c_int, [vp, dp, dp]),
@@ -235,6 +241,28 @@ class Laps:
         eb = np.zeros(nshell)
         self._ck(self.lib.laps_spectrum(self.h, int(nshell), _dptr(eu), _dptr(eb)))
         return eu, eb
+
+    # -- granular path (the reference's subroutines one at a time)
+    def nflux(self) -> int:
+        return 18 + (1 if self.p.if_AEB else 0)
+
+    def calc_flux(self) -> np.ndarray:
+        out = np.empty((self.nflux(),) + self.shape)
+        self._ck(self.lib.laps_calc_flux(self.h, _dptr(out)))
+        return out
+
+    def transform_flux(self) -> np.ndarray:
+        out = np.empty((self.nflux(),) + self.shape[:2] + (self.shape[2] // 2 + 1,), dtype=np.complex128)
+        self._ck(self.lib.laps_transform_flux(self.h, _dptr(out.view(np.float64))))
+        return out
+
+    def calc_rhs(self) -> np.ndarray:
+        out = np.empty((8,) + self.shape[:2] + (self.shape[2] // 2 + 1,), dtype=np.complex128)
+        self._ck(self.lib.laps_calc_rhs(self.h, _dptr(out.view(np.float64))))
+        return out
+
+    def dealias(self):
+        self._ck(self.lib.laps_dealias(self.h))
 
     def write_output(self, path, primitive: bool = True):
         """Write the state as the reference's outNNN.dat."""
