@@ -125,6 +125,37 @@ module laps_gpu
             import :: c_ptr
             type(c_ptr), value :: batch
         end subroutine
+        integer(c_int) function laps_write_output(ctx, path, layout) bind(C, name='laps_write_output')
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated, e.g. 'out007.dat'//c_null_char
+            integer(c_int), value :: layout
+        end function
+        integer(c_int) function laps_read_restart(ctx, path, time) bind(C, name='laps_read_restart')
+            import :: c_int, c_ptr, c_char, c_double
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+            real(c_double), intent(out) :: time
+        end function
+        integer(c_int) function laps_calc_flux(ctx, flux) bind(C, name='laps_calc_flux')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: flux(*)
+        end function
+        integer(c_int) function laps_transform_flux(ctx, flux_fourier) bind(C, name='laps_transform_flux')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: flux_fourier(*)
+        end function
+        integer(c_int) function laps_calc_rhs(ctx, fnl) bind(C, name='laps_calc_rhs')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: fnl(*)
+        end function
+        integer(c_int) function laps_dealias(ctx) bind(C, name='laps_dealias')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
         integer(c_int) function laps_wait(ctx, timeout_ms) bind(C, name='laps_wait')
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx
