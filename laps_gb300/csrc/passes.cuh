@@ -545,13 +545,41 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   // FP32 minimum (or FP32 NaN) in the state type TS.  The screened value of a point's bound is
   // within 1e-5 of its TS value, so the block's TS minimum is the one a full TS evaluation
   // gives.
+  constexpr int MAXC = 32;
+  __shared__ SR cand[CFL ? MAXC : 1][NQ];
+  __shared__ int ncand;
+  bool cand_late = false;  // block-uniform: the list waits for warp 0 at the end
+  using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
+  const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
+  auto report = [&](TS tmin, bool nan_seen) {  // warp min, then one atomic per warp
+    double dmin = Real<TS>::to_d(tmin);
+    for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+    const bool any_nan = __any_sync(0xffffffffu, nan_seen);
+    if ((threadIdx.x & 31) == 0) {
+      if (any_nan) atomicOr(&a.st->status, LAPS_STATUS_NAN);
+      atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(dmin));
+    }
+  };
+  // warp 0: the candidate list in TS
+  auto eval_list = [&]() {
+    if (threadIdx.x >= 32) return;
+    TS tmin = Real<TS>::inf();
+    bool nan_seen = false;
+    if ((int)threadIdx.x < ncand) {
+      TS qs[NQ];
+#pragma unroll
+      for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(&cand[threadIdx.x][f])) : kk.ps.zero;
+      const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
+      if (Real<TS>::isnan_(d)) nan_seen = true;
+      else tmin = d;
+    }
+    report(tmin, nan_seen);
+  };
   if (CFL) {
     using PHF = typename std::conditional<INCOMP, FluxI<float>, Flux<float>>::type;
-    using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
     __shared__ float red32[32];
     const PT<float> pf = pt_float(pc);
     const float rfac_f = (float)(a.st->radius / a.P.R0);
-    const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
     constexpr int PPT = (CF::ROWS * NX + CF::THREADS - 1) / CF::THREADS;  // points per thread
     float d32[PPT];
     float m32 = __int_as_float(0x7f800000);
@@ -569,10 +597,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       }
     }
     // candidates: the points within 0.01 % of the block's FP32 minimum, and FP32 NaNs; their
-    // inputs are copied to a list that one warp evaluates in TS while the others go on
-    constexpr int MAXC = 32;
-    __shared__ SR cand[MAXC][NQ];
-    __shared__ int ncand;
+    // inputs are copied to a list that one warp evaluates in TS after its other work
     if (threadIdx.x == 0) ncand = 0;
     for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
     if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = m32;
@@ -592,29 +617,9 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     }
     __syncthreads();  // the list is complete; the physics may now overwrite the inputs
     const int nc = ncand;
-    auto report = [&](TS tmin, bool nan_seen) {  // warp min, then one atomic per warp
-      double dmin = Real<TS>::to_d(tmin);
-      for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
-      const bool any_nan = __any_sync(0xffffffffu, nan_seen);
-      if ((threadIdx.x & 31) == 0) {
-        if (any_nan) atomicOr(&a.st->status, LAPS_STATUS_NAN);
-        atomicMin(&a.st->cfl_bits, (unsigned long long)__double_as_longlong(dmin));
-      }
-    };
     if (nc <= MAXC) {
-      if (threadIdx.x < 32) {
-        TS tmin = Real<TS>::inf();
-        bool nan_seen = false;
-        if ((int)threadIdx.x < nc) {
-          TS qs[NQ];
-#pragma unroll
-          for (int f = 0; f < NQ; f++) qs[f] = f < nin ? Cvt<TS, T>::r(Store<T>::ld(&cand[threadIdx.x][f])) : kk.ps.zero;
-          const TS d = PHS::cfl(qs, kk.ps, a.P, rfac);
-          if (Real<TS>::isnan_(d)) nan_seen = true;
-          else tmin = d;
-        }
-        report(tmin, nan_seen);
-      }
+      // the list is evaluated by warp 0 at the end of the kernel, off the physics' barrier
+      cand_late = true;
     } else {  // more candidates than the list holds: every thread evaluates its own
       TS tmin = Real<TS>::inf();
       bool nan_seen = false;
@@ -634,7 +639,10 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       __syncthreads();  // before the physics overwrites the inputs
     }
   }
-  if (nfl == 0) return;
+  if (nfl == 0) {
+    if (CFL && cand_late) eval_list();
+    return;
+  }
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
   const T inv_tau = Real<T>::from_d(a.st->inv_tau);
   const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
@@ -676,6 +684,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       }
     }
   }
+  if (CFL && cand_late) eval_list();  // after this warp's share of the transforms
 }
 
 // Resident blocks per SM the register budget of passes D and E is set for (FP32 lines): 5
