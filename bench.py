@@ -442,7 +442,9 @@ def run_ours(args):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(name)
+            key = f"{args.workload}/{args.precision}"
+            if not SHAPE and n == WL["grid"]:
+                traffic = json.loads(tf.read_text()).get(key, {}).get(name)
         except Exception:
             traffic = None
     line = {

@@ -29,6 +29,37 @@ struct Geo {
   __host__ __device__ bool kz_in(int kz) const { return kz < kz_lo || kz >= kz_hi; }
 };
 
+// Tile copies of a line whose kept rows are [0, lo) U [hi, n): boxes of `box` rows at 0, box,
+// 2 box, ... below lo_end and at n - box, n - 2 box, ... down to hi_start, so that the unkept
+// middle is not fetched.  `box` is a multiple of `gran` rows (n a power of two), so that every
+// copy lands on a 128-byte boundary of shared memory (gran = 128 / tile row bytes).  When the
+// two runs of boxes would overlap (little or no dealiasing) the whole line is copied in boxes
+// of min(n, 256) rows from 0 and the high run is empty.
+struct KeptCopies {
+  int box, lo_end, hi_start;  // low run covers [0, lo_end), high run [hi_start, n)
+  __host__ __device__ KeptCopies(int lo, int hi, int n, int gran) {
+    const int nh = n - hi, full = n < 256 ? n : 256;
+    int kb = lo > nh ? lo : nh;
+    kb = kb < 1 ? 1 : kb;
+    const int parts = (kb + 255) / 256;  // boxes of at most 256 rows, as even as they come
+    kb = (kb + parts - 1) / parts;
+    kb = (kb + gran - 1) / gran * gran;
+    const bool split = kb <= full && (lo + kb - 1) / kb * kb + (nh + kb - 1) / kb * kb <= n;
+    box = split ? kb : full;
+    lo_end = split ? lo : n;
+    hi_start = split ? hi : n;
+  }
+  // number of box copies per line
+  __host__ __device__ int count(int n) const { return (lo_end + box - 1) / box + (n - hi_start + box - 1) / box; }
+  // start row of copy i (i < count(n))
+  __host__ __device__ int start(int i, int n) const {
+    const int nl = (lo_end + box - 1) / box;
+    return i < nl ? i * box : n - (i - nl + 1) * box;
+  }
+};
+// rows of TX complex elements of `bytes` each that make 128 bytes
+__host__ __device__ constexpr int tile_gran(int bytes) { return 128 / (TX * bytes) > 1 ? 128 / (TX * bytes) : 1; }
+
 // ------------------------------------------------------------------------------ step state
 // Written only by device kernels during a step; read by every pass kernel.
 struct StepState {

@@ -141,7 +141,11 @@ template <class T, class TS = T> class Engine : public EngineBase {
   StepState* h_st = nullptr;  // pinned mirror
   double* d_part = nullptr;   // diagnostics partial sums
   CUtensorMap tm_d{}, tm_e{};  // tile copies of pass D (y columns of W1) and E (z columns of W2)
-  CUtensorMap tm_a{};          // pass A: z columns of the state U
+  // pass A: kept kz rows of the z columns of the state U; pass B: kept ky rows of the y
+  // columns of W1.  Index 0 for the whole spectrum, 1 for the pruned one: the box height of
+  // each map is that geometry's KeptCopies box, which the kernel recomputes from its Geo.
+  CUtensorMap tm_a[2]{}, tm_b[2]{};
+  int box_a[2]{}, box_b[2]{};
   int npart = 0;
 
   template <class X> X* dalloc(size_t n) {
@@ -273,7 +277,13 @@ template <class T, class TS = T> class Engine : public EngineBase {
       const int ew = (int)(sizeof(C) / 8);
       tm_d = work_tensor_map(B.W1, g, 19, ew, std::min(q.ny, 256), 1);
       tm_e = work_tensor_map(B.W2, g, w2_fields(q), ew, 1, std::min(q.nz, 256));
-      tm_a = work_tensor_map(B.U, g, 8, (int)(sizeof(CS) / 8), 1, std::min(q.nz, 256));
+      for (int i = 0; i < 2; i++) {
+        const Geo& gk = i ? gprune : gfull;
+        box_a[i] = KeptCopies(gk.kz_lo, gk.kz_hi, q.nz, tile_gran((int)sizeof(CS))).box;
+        box_b[i] = KeptCopies(gk.ky_lo, gk.ky_hi, q.ny, tile_gran((int)sizeof(C))).box;
+        tm_a[i] = work_tensor_map(B.U, g, 8, (int)(sizeof(CS) / 8), 1, box_a[i]);
+        tm_b[i] = work_tensor_map(B.W1, g, 19, ew, box_b[i], 1);
+      }
     }
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
     LAPS_CK(cudaMemsetAsync(B.R, 0, 8 * g.fsc * sizeof(C), stream));
@@ -418,8 +428,18 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.rhs_only = rhs_mode;
     return a;
   }
-  void passA(const PassArgs& a) { launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, &tm_a); }
-  void passB(const PassArgs& a) { launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
+  // the map whose box matches the kept-row copies the kernel makes for a.g
+  const CUtensorMap* kept_map(const CUtensorMap* m, const int* box, int want) const {
+    if (box[1] == want) return &m[1];
+    if (box[0] == want) return &m[0];
+    throw Error{LAPS_EINVAL, "no tile map for this geometry"};
+  }
+  void passA(const PassArgs& a) {
+    launch_passA<T, TS>(stream, p.nz, B, a, passk(), twz, kept_map(tm_a, box_a, KeptCopies(a.g.kz_lo, a.g.kz_hi, p.nz, tile_gran((int)sizeof(CS))).box));
+  }
+  void passB(const PassArgs& a) {
+    launch_passB<T, TS>(stream, p.ny, B, a, passk(), twy, kept_map(tm_b, box_b, KeptCopies(a.g.ky_lo, a.g.ky_hi, p.ny, tile_gran((int)sizeof(C))).box));
+  }
   void passC(const PassArgs& a) { launch_passC<T, TS>(stream, p.nx, B, a, passk(), twx); }
   void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passE(const PassArgs& a) {

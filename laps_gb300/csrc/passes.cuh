@@ -82,13 +82,19 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
     TileLoad tl;
     tl.init(tbar);
     if (threadIdx.x == 0) {
-      constexpr int EW = (int)(sizeof(CS) / 8), ZB = NZ < 256 ? NZ : 256;
+      // only the kept kz rows of each column (the map's box is kc.box rows high)
+      constexpr int EW = (int)(sizeof(CS) / 8);
+      const KeptCopies kc(g.kz_lo, g.kz_hi, NZ, tile_gran((int)sizeof(CS)));
+      const int nc = kc.count(NZ);
       const int r0 = blockIdx.y * CL::NTILE;
       const int nt = g.nky() - r0 < CL::NTILE ? g.nky() - r0 : CL::NTILE;
-      tl.expect(0, (uint32_t)(nt * NZ * TX * (int)sizeof(CS)));
+      tl.expect(0, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(CS)));
       for (int t = 0; t < nt; t++) {
         CS* dst = reinterpret_cast<CS*>(smem_tma + CL::NTILE * NZ * TX * (int)sizeof(C)) + t * NZ * TX;
-        for (int z0 = 0; z0 < NZ; z0 += ZB) tl.copy(0, dst + z0 * TX, &tmap, blockIdx.x * TX * EW, g.ky_of(r0 + t), e.src * g.nz + z0);
+        for (int i = 0; i < nc; i++) {
+          const int z0 = kc.start(i, NZ);
+          tl.copy(0, dst + z0 * TX, &tmap, blockIdx.x * TX * EW, g.ky_of(r0 + t), e.src * g.nz + z0);
+        }
       }
     }
     if (!tl.wait(0, a.st)) return;
@@ -174,15 +180,20 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS)
     tl.init(tbar);
     const int nin = e.in1 >= 0 ? 2 : 1;
     if (threadIdx.x == 0) {
-      constexpr int EW = (int)(sizeof(C) / 8), YB = NY < 256 ? NY : 256;
+      // only the kept ky rows of each column (the map's box is kc.box rows high)
+      constexpr int EW = (int)(sizeof(C) / 8);
+      const KeptCopies kc(g.ky_lo, g.ky_hi, NY, tile_gran((int)sizeof(C)));
+      const int nc = kc.count(NY);
       const int z0 = blockIdx.y * CL::NTILE;
       const int nt = g.nz - z0 < CL::NTILE ? g.nz - z0 : CL::NTILE;
       for (int k = 0; k < nin; k++) {
-        tl.expect(k, (uint32_t)(nt * NY * TX * (int)sizeof(C)));
+        tl.expect(k, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(C)));
         for (int t = 0; t < nt; t++) {
           C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + k) * NY * TX;  // tile t, buffer k
-          for (int y0 = 0; y0 < NY; y0 += YB)
+          for (int i = 0; i < nc; i++) {
+            const int y0 = kc.start(i, NY);
             tl.copy(k, dst + y0 * TX, &tmap, blockIdx.x * TX * EW, y0, (k == 0 ? e.in0 : e.in1) * g.nz + z0 + t);
+          }
         }
       }
     }
