@@ -73,7 +73,7 @@ struct StepState {
   int status;                      // LAPS_STATUS_* bits
   int halt;                        // skip the rest of the step (dt floor)
   int ksq_plain;                   // k^2 still the grid_initialize sum (no R factor)
-  int pad;
+  unsigned int cfl32_bits;         // running min of the FP32 screen of the CFL step (bits of a float)
 };
 
 // wave-number tables (element type T), rebuilt by a small kernel whenever R changes

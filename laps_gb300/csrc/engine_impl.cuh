@@ -340,6 +340,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     s0.inv_tau = P.Ur != 0.0 ? 1.0 / (q.radius0 / P.Ur) : 0.0;
     s0.r_ratio = 1.0;  // radius0 / radius at start; the factor itself is (k R0)/R below
     s0.cfl_bits = 0x7FF0000000000000ull;
+    s0.cfl32_bits = 0x7F800000u;
     s0.ksq_plain = 1;  // grid_initialize's k^2 until the first evolve_radius
     s0.rho0 = q.rho0 > 0 ? q.rho0 : 1.0;
     s0.istep = 0;

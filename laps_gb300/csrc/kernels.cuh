@@ -377,6 +377,7 @@ static __global__ void k_finalize_dt(StepState* st, double cfl, int dstep, int l
   if (st->halt) return;
   double m = __longlong_as_double((long long)st->cfl_bits);
   st->cfl_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
+  st->cfl32_bits = 0x7F800000u;
   if (!force && dstep > 1 && st->istep % dstep != 0) return;
   double dtmin = m * cfl;
   double dt = st->dt;

@@ -555,10 +555,13 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   // approximate divide and square root, then only the points within 0.01 % of the block's
   // FP32 minimum (or FP32 NaN) in the state type TS.  The screened value of a point's bound is
   // within 1e-5 of its TS value, so the block's TS minimum is the one a full TS evaluation
-  // gives.
+  // gives.  Blocks also publish their FP32 minimum to the step's running minimum: a block
+  // whose minimum lies above 1.0001 times a published one holds no point whose TS bound can be
+  // the step's minimum and evaluates nothing in TS (the block with the smallest published
+  // minimum always evaluates, and so does every block with an FP32 NaN).
   constexpr int MAXC = 32;
   __shared__ SR cand[CFL ? MAXC : 1][NQ];
-  __shared__ int ncand;
+  __shared__ int ncand, skip_ts;
   bool cand_late = false;  // block-uniform: the list waits for warp 0 at the end
   using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
   const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
@@ -594,6 +597,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     constexpr int PPT = (CF::ROWS * NX + CF::THREADS - 1) / CF::THREADS;  // points per thread
     float d32[PPT];
     float m32 = __int_as_float(0x7f800000);
+    bool nan32 = false;
 #pragma unroll
     for (int i = 0; i < PPT; i++) {
       const int p = threadIdx.x + i * CF::THREADS;
@@ -605,6 +609,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
         for (int f = 0; f < NQ; f++) qf[f] = f < nin ? Cvt<float, T>::r(Store<T>::ld(base + f * CF::FSTR)) : 0.f;
         d32[i] = PHF::cfl_screen(qf, pf, a.P, rfac_f);
         m32 = fminf(m32, d32[i]);
+        nan32 |= isnan(d32[i]);
       }
     }
     // candidates: the points within 0.01 % of the block's FP32 minimum, and FP32 NaNs; their
@@ -612,9 +617,18 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     if (threadIdx.x == 0) ncand = 0;
     for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
     if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = m32;
-    __syncthreads();
+    const bool any_nan = __syncthreads_or(nan32) != 0;
     for (int w = 0; w < CF::THREADS / 32; w++) m32 = fminf(m32, red32[w]);
     const float thr = m32 * 1.0001f;
+    if (threadIdx.x == 0) {
+      // bounds are positive (or +inf), so their float bits order as unsigned integers
+      bool skip = false;
+      if (m32 >= 0.f) {
+        const unsigned int old = atomicMin(&a.st->cfl32_bits, __float_as_uint(m32));
+        skip = !any_nan && m32 > 1.0001f * __uint_as_float(old);
+      }
+      skip_ts = skip;
+    }
 #pragma unroll
     for (int i = 0; i < PPT; i++) {
       const int p = threadIdx.x + i * CF::THREADS;
@@ -628,13 +642,15 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     }
     __syncthreads();  // the list is complete; the physics may now overwrite the inputs
     const int nc = ncand;
-    if (nc <= MAXC) {
+    if (skip_ts) {
+      // another block's FP32 minimum is below this block's by more than the screen's error
+    } else if (nc <= MAXC) {
       // the list is evaluated by warp 0 at the end of the kernel, off the physics' barrier
       cand_late = true;
     } else {  // more candidates than the list holds: every thread evaluates its own
       TS tmin = Real<TS>::inf();
       bool nan_seen = false;
-#pragma unroll 1
+#pragma unroll
       for (int i = 0; i < PPT; i++) {
         const int p = threadIdx.x + i * CF::THREADS;
         if (p >= CF::ROWS * NX || (!(d32[i] <= thr) && !isnan(d32[i]))) continue;
