@@ -136,6 +136,50 @@ void laps_destroy(laps_ctx* ctx);
  * (mhdinit.f90:1038-1056) + transform_uu_real_to_fourier (fftw.f90:42-71, mhd.f90:121-122). */
 int laps_upload_state(laps_ctx* ctx, const double* uu, int layout);
 
+/*
+ * Initial-condition parameters: the user-defined namelist values of mhdinit.f90:13-14,48-55
+ * (src_compressible; src_incompressible/mhdinit.f90 has the same names).  laps_ic_default
+ * fills the reference's module initialisers (T0 = rho0 = B0 = 1, a0 = 0.05,
+ * in_out_ratio = 1, nmode* = 16, jet_width = 1, Vjet = 0.3, wave_number_jet = 1, rest 0).
+ */
+typedef struct laps_ic {
+  int ifield; /* background: 0 uniform rho0 / rho0*T0, 1 double current sheet Bx(z), 2 double
+                 Harris shear ux(y), 3 uniform B, 4 double current sheet Bx(y) at constant
+                 density, 5 jet along x (3-D compressible only) */
+  int ipert;  /* perturbation: 0 none, 1 circularly polarised Alfven wave, 6 outward and inward
+                 Alfvenic waves, 7 random-phase u, B, rho modes, 8 switchback */
+  double T0, rho0, B0, a0;
+  double U_fast, U_slow, n_fast, n_slow, press0, shear_width;
+  double bx0, by0, bz0, db0, in_out_ratio, dv0, drho0;
+  int nmodex, nmodey, nmodez, wave_number_jet;
+  double jet_width, Vjet;
+  double B0_SB, dB_SB, R0_SB, R1_SB, H_SB, Rm_SB, Rd_SB;
+} laps_ic;
+
+/* Fill *ic with the reference's defaults. */
+int laps_ic_default(laps_ic* ic);
+
+/* Number of phases laps_init_fields reads for ic (0 for the deterministic cases):
+ *   ipert 6: 2 * nmodex * (2 nmodey + 1) * (2 nmodez + 1)  (outward waves, then inward waves)
+ *   ipert 7: 3 * (2 nmodex + 1) * (2 nmodey + 1) * (2 nmodez + 1)  (u, B, rho phases)
+ * indexed as the reference's phs arrays (mhdinit.f90:523-526,594-597,762-769) without the
+ * Fortran 1. */
+long long laps_ic_nphases(const laps_ic* ic);
+
+/*
+ * Generate the initial state on the device: background_fields_initialize (mhdinit.f90:183-299)
+ * + perturbation_initialize for ipert 1, 6, 7, 8 (:302-342,487-688,690-930,931-1019) +
+ * initial_calc_conserve_variable (:1038-1056) + transform_uu_real_to_fourier, i.e. what
+ * mhd.f90:110-122 does on a fresh start.  The reference draws the phases of ipert 6 and 7
+ * with the compiler's random_number; here they are an input (radians, laps_ic_nphases of
+ * them; NULL when there are none), so any generator can supply them.  The random-phase
+ * modes are placed in the half spectrum and transformed with the state's inverse transform
+ * instead of summed point by point; they need |k| < n/2 on every axis (nmodex < nx/2 ...).
+ * ipert 2-5 (random 1-D / modulated perturbations) are not built: LAPS_EINVAL.
+ * 3-D variants only (the 2-D code has its own initial conditions): LAPS_EINVAL for 2-D.
+ */
+int laps_init_fields(laps_ctx* ctx, const laps_ic* ic, const double* phases, long long nphases);
+
 /* Set the simulation time and the expanding-box radius: evolve_radius(t)
  * (AEBmod.f90:56-73,87-125), as the restart path does (mhd.f90:101-103). */
 int laps_set_time(laps_ctx* ctx, double time);

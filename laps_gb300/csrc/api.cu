@@ -128,6 +128,48 @@ int laps_upload_state(laps_ctx* c, const double* uu, int layout) {
   if (!uu || (layout != LAPS_LAYOUT_PRIMITIVE && layout != LAPS_LAYOUT_CONSERVED)) return fail(c, LAPS_EINVAL, "bad state pointer or layout");
   return guarded(c, [&] { c->e->upload(uu, layout); });
 }
+int laps_ic_default(laps_ic* ic) {
+  if (!ic) return LAPS_EINVAL;
+  std::memset(ic, 0, sizeof(*ic));
+  ic->T0 = 1.0; ic->rho0 = 1.0;  // mhdinit.f90:13
+  ic->B0 = 1.0; ic->a0 = 0.05;   // mhdinit.f90:14
+  ic->in_out_ratio = 1.0;        // mhdinit.f90:48-49
+  ic->nmodex = ic->nmodey = ic->nmodez = 16;  // mhdinit.f90:50
+  ic->jet_width = 1.0; ic->Vjet = 0.3; ic->wave_number_jet = 1;  // mhdinit.f90:52-53
+  return LAPS_OK;
+}
+long long laps_ic_nphases(const laps_ic* ic) {
+  if (!ic) return 0;
+  const long long mx = ic->nmodex, my = ic->nmodey, mz = ic->nmodez;
+  if (ic->ipert == 6) return 2 * mx * (2 * my + 1) * (2 * mz + 1);
+  if (ic->ipert == 7) return 3 * (2 * mx + 1) * (2 * my + 1) * (2 * mz + 1);
+  return 0;
+}
+int laps_init_fields(laps_ctx* c, const laps_ic* ic, const double* phases, long long nphases) {
+  if (!c) return LAPS_EINVAL;
+  if (!ic) return fail(c, LAPS_EINVAL, "null initial-condition parameters");
+  const laps_params& q = c->e->params();
+  if (q.variant == LAPS_VARIANT_2DC) return fail(c, LAPS_EINVAL, "initial conditions are generated for the 3-D variants only");
+  if (ic->ifield < 0 || ic->ifield > 5 || (ic->ifield == 5 && q.variant != LAPS_VARIANT_3DC))
+    return fail(c, LAPS_EINVAL, "ifield must be 0-4 (0-5 for the 3-D compressible variant)");
+  if (ic->ipert != 0 && ic->ipert != 1 && ic->ipert != 6 && ic->ipert != 7 && ic->ipert != 8)
+    return fail(c, LAPS_EINVAL, "ipert must be 0, 1, 6, 7 or 8 (2-5 are not built)");
+  if ((ic->ifield == 1 || ic->ifield == 4) && ic->a0 == 0.0) return fail(c, LAPS_EINVAL, "a0 = 0");
+  if (ic->ifield == 2 && ic->shear_width == 0.0) return fail(c, LAPS_EINVAL, "shear_width = 0");
+  if (ic->ifield == 1 && ic->T0 == 0.0) return fail(c, LAPS_EINVAL, "T0 = 0");
+  if (ic->ipert == 8 && (ic->R1_SB == 0.0 || ic->H_SB == 0.0 || ic->Rd_SB == 0.0))
+    return fail(c, LAPS_EINVAL, "switchback widths R1_SB, H_SB, Rd_SB must be non-zero");
+  const long long need = laps_ic_nphases(ic);
+  if (need > 0) {
+    if (ic->nmodex < 1 || ic->nmodey < 0 || ic->nmodez < 0) return fail(c, LAPS_EINVAL, "nmodex >= 1, nmodey, nmodez >= 0");
+    if (2 * ic->nmodex >= q.nx || 2 * ic->nmodey >= q.ny || 2 * ic->nmodez >= q.nz)
+      return fail(c, LAPS_EINVAL, "random-phase modes need nmodex < nx/2, nmodey < ny/2, nmodez < nz/2");
+    if (!phases || nphases != need) return fail(c, LAPS_EINVAL, "phases: laps_ic_nphases(ic) values expected");
+    if (ic->ipert == 7 && ic->bx0 == 0.0 && ic->by0 == 0.0 && ic->bz0 == 0.0)
+      return fail(c, LAPS_EINVAL, "ipert 7 needs a non-zero background field (bx0, by0, bz0)");
+  }
+  return guarded(c, [&] { c->e->init_fields(*ic, phases); });
+}
 int laps_set_time(laps_ctx* c, double t) { return guarded(c, [&] { c->e->set_time(t); }); }
 int laps_vardt(laps_ctx* c, double* dt) {
   return guarded(c, [&] {

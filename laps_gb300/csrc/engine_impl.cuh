@@ -10,8 +10,12 @@
 #include <chrono>
 #include <cudaTypedefs.h>
 #include <thread>
+#include <map>
+#include <array>
+#include <complex>
 #include "launch.cuh"
 #include "diag.cuh"
+#include "ic.cuh"
 
 namespace laps {
 
@@ -102,10 +106,13 @@ class EngineBase {
   virtual const double* stage_real_state() = 0;
   virtual long long grid_points() const = 0;
   virtual int variant() const = 0;
+  virtual const laps_params& params() const = 0;
   // granular, unfused path (bisection against the reference's subroutines)
   virtual void calc_flux(double* host, int spectral) = 0;
   virtual void calc_rhs(double* host) = 0;
   virtual void dealias_state() = 0;
+  // fresh-start initial conditions generated on the device (phases of ipert 6 / 7 given)
+  virtual void init_fields(const laps_ic& ic, const double* phases) = 0;
 };
 
 // T: compute type of the transforms and products; TS: storage type of the state, the RK
@@ -574,6 +581,121 @@ template <class T, class TS = T> class Engine : public EngineBase {
     have_state = true;
     wait(tmo());
   }
+  void init_fields(const laps_ic& ic, const double* ph) override {
+    const Geo& g = gfull;
+    IcDev d{};
+    d.ic = ic;
+    d.Lx = p.Lx; d.Ly = p.Ly; d.Lz = p.Lz;
+    d.cosc = P.cos_cor; d.sinc = P.sin_cor;
+    d.gamma = P.gamma;
+    d.incomp = P.variant == LAPS_VARIANT_3DI;
+    d.modes = ic.ipert == 6 || ic.ipert == 7;
+    if (d.modes) {
+      // the mode sums as half-spectrum coefficients: A cos(k.x + phi) is A/2 e^{i phi} at k
+      // (and its conjugate at -k, stored explicitly on the kx = 0 plane); modes that meet
+      // at one wave vector add up
+      std::map<long long, std::array<std::complex<double>, 7>> acc;
+      auto put = [&](int f, int ikx, int iky, int ikz, std::complex<double> c) {
+        const long long yi = ((iky % p.ny) + p.ny) % p.ny, zi = ((ikz % p.nz) + p.nz) % p.nz;
+        const long long key = (zi * p.ny + yi) * g.kxp + ikx;
+        auto it = acc.find(key);
+        if (it == acc.end()) it = acc.emplace(key, std::array<std::complex<double>, 7>{}).first;
+        it->second[f] += c;
+      };
+      auto add = [&](int f, int ikx, int iky, int ikz, double A, double phi) {
+        if (ikx < 0 || (ikx == 0 && (iky < 0 || (iky == 0 && ikz < 0)))) {
+          ikx = -ikx; iky = -iky; ikz = -ikz; phi = -phi;
+        }
+        const std::complex<double> c = 0.5 * A * std::polar(1.0, phi);
+        put(f, ikx, iky, ikz, c);
+        if (ikx == 0) put(f, 0, -iky, -ikz, std::conj(c));
+      };
+      const double pi = 3.141592653589793, half_pi = 0.5 * pi;
+      const int mx = ic.nmodex, my = ic.nmodey, mz = ic.nmodez;
+      if (ic.ipert == 6) {  // mhdinit.f90:487-634: outward waves, then inward ones
+        const long long nm = (long long)mx * (2 * my + 1) * (2 * mz + 1);
+        const double sgn = std::copysign(1.0, ic.bx0);
+        for (int w = 0; w < 2; w++) {
+          const int dirx = w ? -1 : 1;
+          const double su = w ? 1.0 : -1.0, io = w ? ic.in_out_ratio : 1.0;
+          for (int ikx = 1; ikx <= mx; ikx++)
+            for (int iky = -my; iky <= my; iky++)
+              for (int ikz = -mz; ikz <= mz; ikz++) {
+                const double ax = std::sqrt(1 / (double)ikx), ay = iky == 0 ? 1.0 : std::sqrt(1 / (double)std::abs(iky)),
+                             az = ikz == 0 ? 1.0 : std::sqrt(1 / (double)std::abs(ikz));
+                const double a = ax * ay * az * io;
+                const double ph0 = ph[w * nm + ((long long)(ikx - 1) * (2 * my + 1) + iky + my) * (2 * mz + 1) + ikz + mz];
+                const int kx = dirx * ikx;
+                if (iky == 0 && ikz == 0) {
+                  add(5, kx, 0, 0, ic.db0 * a, ph0);
+                  add(6, kx, 0, 0, ic.db0 * a, ph0 - half_pi);
+                  add(2, kx, 0, 0, su * sgn * ic.db0 * a, ph0);
+                  add(3, kx, 0, 0, su * sgn * ic.db0 * a, ph0 - half_pi);
+                } else {
+                  const double ky = iky * 2 * pi / p.Ly, kz = ikz * 2 * pi / p.Lz, kk = std::sqrt(ky * ky + kz * kz);
+                  const double dby = ic.db0 * kz / kk, dbz = -ic.db0 * ky / kk;
+                  add(5, kx, iky, ikz, dby * a, ph0);
+                  add(6, kx, iky, ikz, dbz * a, ph0);
+                  add(2, kx, iky, ikz, su * sgn * dby * a, ph0);
+                  add(3, kx, iky, ikz, su * sgn * dbz * a, ph0);
+                }
+              }
+        }
+      } else {  // mhdinit.f90:690-930: u, B, rho modes perpendicular to k and B0
+        const long long nm = (long long)(2 * mx + 1) * (2 * my + 1) * (2 * mz + 1);
+        const double corr = -0.05;
+        const double B0mod = std::sqrt(ic.bx0 * ic.bx0 + ic.by0 * ic.by0 + ic.bz0 * ic.bz0);
+        const int mmax = std::max(mx, std::max(my, mz));
+        for (int ikx = 0; ikx <= mx; ikx++)
+          for (int iky = -my; iky <= my; iky++)
+            for (int ikz = -mz; ikz <= mz; ikz++) {
+              if ((ikx == 0 && iky < 0) || (ikx == 0 && iky == 0 && ikz <= 0)) continue;
+              const double kr = std::sqrt((double)(ikx * ikx + iky * iky + ikz * ikz));
+              if (kr > mmax) continue;
+              const double kx = ikx * 2 * pi / p.Lx, ky = iky * 2 * pi / p.Ly, kz = ikz * 2 * pi / p.Lz;
+              const double kmod = std::sqrt(kx * kx + ky * ky + kz * kz);
+              const double dv[3] = {(ky * ic.bz0 - kz * ic.by0) / kmod / B0mod, (kz * ic.bx0 - kx * ic.bz0) / kmod / B0mod,
+                                    (kx * ic.by0 - ky * ic.bx0) / kmod / B0mod};
+              const long long j = ((long long)(ikx + mx) * (2 * my + 1) + iky + my) * (2 * mz + 1) + ikz + mz;
+              const double ph0 = ph[j], ph1 = ph[nm + j], ph2 = ph[2 * nm + j];
+              const double kr3 = std::sqrt(kr * kr * kr);
+              for (int c = 0; c < 3; c++) add(1 + c, ikx, iky, ikz, std::sqrt(1 - corr * corr) * ic.dv0 / kr3 * dv[c], ph0);
+              for (int c = 0; c < 3; c++) add(4 + c, ikx, iky, ikz, ic.db0 / kr3 * dv[c], ph1);
+              for (int c = 0; c < 3; c++) add(1 + c, ikx, iky, ikz, corr * ic.dv0 / kr3 * dv[c], ph1);
+              add(0, ikx, iky, ikz, ic.drho0 / kr3, ph2);
+            }
+      }
+      std::vector<long long> hidx;
+      std::vector<double2> hval;
+      for (auto& kv : acc) {
+        hidx.push_back(kv.first);
+        for (int f = 0; f < 7; f++) hval.push_back(make_double2(kv.second[f].real(), kv.second[f].imag()));
+      }
+      LAPS_CK(cudaMemsetAsync(B.U, 0, 7 * g.fsc * sizeof(CS), stream));
+      const int cnt = (int)hidx.size();
+      if (cnt > 0) {
+        long long* didx = nullptr;
+        double2* dval = nullptr;
+        LAPS_CK(cudaMalloc(&didx, hidx.size() * sizeof(long long)));
+        LAPS_CK(cudaMalloc(&dval, hval.size() * sizeof(double2)));
+        LAPS_CK(cudaMemcpyAsync(didx, hidx.data(), hidx.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
+        LAPS_CK(cudaMemcpyAsync(dval, hval.data(), hval.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
+        k_place_modes<TS><<<(cnt + 255) / 256, 256, 0, stream>>>(B.U, g.fsc, didx, dval, cnt);
+        LAPS_CK(cudaGetLastError());
+        wait(tmo());
+        LAPS_CK(cudaFree(didx));
+        LAPS_CK(cudaFree(dval));
+      }
+      inverse3d(B.U, 7);  // the mode sums on the grid: W1 real fields 0..6
+    }
+    k_init_fields<TS><<<1024, 256, 0, stream>>>((SRS*)B.W1, g, d);
+    LAPS_CK(cudaGetLastError());
+    forward3d((const SRS*)B.W1, B.U, 8);
+    LAPS_CK(cudaMemsetAsync(&st->dt, 0, sizeof(double), stream));
+    dealiased = false;
+    have_state = true;
+    wait(tmo());
+  }
   void set_time(double t) override {
     read_state();  // sync mirror
     StepState s = *h_st;
@@ -657,6 +779,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     LAPS_CK(cudaGetLastError());
     return out;
   }
+  const laps_params& params() const override { return p; }
   long long grid_points() const override { return gfull.fsr; }
   int variant() const override { return P.variant; }
   void download(double* uu, double* prim) override {

@@ -61,6 +61,34 @@ class laps_diag(C.Structure):
     ]
 
 
+class laps_ic(C.Structure):
+    _fields_ = [
+        ("ifield", C.c_int), ("ipert", C.c_int),
+        ("T0", C.c_double), ("rho0", C.c_double), ("B0", C.c_double), ("a0", C.c_double),
+        ("U_fast", C.c_double), ("U_slow", C.c_double), ("n_fast", C.c_double), ("n_slow", C.c_double),
+        ("press0", C.c_double), ("shear_width", C.c_double),
+        ("bx0", C.c_double), ("by0", C.c_double), ("bz0", C.c_double), ("db0", C.c_double),
+        ("in_out_ratio", C.c_double), ("dv0", C.c_double), ("drho0", C.c_double),
+        ("nmodex", C.c_int), ("nmodey", C.c_int), ("nmodez", C.c_int), ("wave_number_jet", C.c_int),
+        ("jet_width", C.c_double), ("Vjet", C.c_double),
+        ("B0_SB", C.c_double), ("dB_SB", C.c_double), ("R0_SB", C.c_double), ("R1_SB", C.c_double),
+        ("H_SB", C.c_double), ("Rm_SB", C.c_double), ("Rd_SB", C.c_double),
+    ]
+
+
+def ic_params(**kw) -> laps_ic:
+    """Initial-condition parameters: the reference's defaults (``laps_ic_default``) overridden
+    by keyword arguments (the namelist names of mhdinit.f90)."""
+    lib = load()
+    ic = laps_ic()
+    lib.laps_ic_default(C.byref(ic))
+    for k, v in kw.items():
+        if not hasattr(ic, k):
+            raise KeyError(k)
+        setattr(ic, k, v)
+    return ic
+
+
 class laps_info(C.Structure):
     _fields_ = [
         ("device_bytes", C.c_longlong), ("kx_keep", C.c_int), ("ky_keep", C.c_int), ("kz_keep", C.c_int),
@@ -91,6 +119,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_create": (C.c_int, [P(laps_params), P(vp)]),
         "laps_destroy": (None, [vp]),
         "laps_upload_state": (C.c_int, [vp, dp, C.c_int]),
+        "laps_ic_default": (C.c_int, [P(laps_ic)]),
+        "laps_ic_nphases": (C.c_longlong, [P(laps_ic)]),
+        "laps_init_fields": (C.c_int, [vp, P(laps_ic), dp, C.c_longlong]),
         "laps_set_time": (C.c_int, [vp, C.c_double]),
         "laps_vardt": (C.c_int, [vp, dp]),
         "laps_step": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
@@ -190,6 +221,16 @@ class Laps:
         a = np.ascontiguousarray(uu, dtype=np.float64)
         assert a.shape == (8,) + self.shape
         self._ck(self.lib.laps_upload_state(self.h, _dptr(a), LAYOUT_PRIMITIVE if primitive else LAYOUT_CONSERVED))
+
+    def init_fields(self, ic: "laps_ic", phases=None):
+        """Generate the fresh-start state on the device (background + perturbation +
+        conserved form + forward transform); ``phases`` (radians) for ipert 6 and 7."""
+        n = self.lib.laps_ic_nphases(C.byref(ic))
+        if n:
+            a = np.ascontiguousarray(phases, dtype=np.float64).ravel()
+            self._ck(self.lib.laps_init_fields(self.h, C.byref(ic), _dptr(a), int(a.size)))
+        else:
+            self._ck(self.lib.laps_init_fields(self.h, C.byref(ic), None, 0))
 
     def set_time(self, t: float):
         self._ck(self.lib.laps_set_time(self.h, float(t)))

@@ -166,3 +166,20 @@ def taylor_green_ic(n, seed=2, kmin=1, kmax=6, alpha=-5.0 / 6.0, rms=1.0, rho0=1
     prim[4:7] = b
     prim[7] = p0
     return prim
+
+
+def ic_phases(ipert: int, nmodex: int, nmodey: int, nmodez: int, seed: int = 0) -> np.ndarray:
+    """Phases (radians, uniform on [0, 2 pi)) for the random-phase perturbations of
+    ``laps_init_fields``: ipert 6 reads the outward then the inward waves' phases, ipert 7 the
+    u, B and rho phases, each in the order of the reference's ``phs`` arrays
+    (``src_compressible/mhdinit.f90:523-526,594-597,762-769``).  The reference draws them with
+    the Fortran compiler's ``random_number``, whose sequence depends on the compiler; this is a
+    seeded ``np.random.default_rng`` stand-in.
+    """
+    if ipert == 6:
+        n = 2 * nmodex * (2 * nmodey + 1) * (2 * nmodez + 1)
+    elif ipert == 7:
+        n = 3 * (2 * nmodex + 1) * (2 * nmodey + 1) * (2 * nmodez + 1)
+    else:
+        return np.zeros(0)
+    return np.random.default_rng(seed).random(n) * 2 * PI
