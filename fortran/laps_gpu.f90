@@ -38,6 +38,16 @@ module laps_gpu
         integer(c_int) :: reserved(8)
     end type laps_params
 
+    type, bind(C) :: laps_ic
+        integer(c_int) :: ifield, ipert
+        real(c_double) :: T0, rho0, B0, a0
+        real(c_double) :: U_fast, U_slow, n_fast, n_slow, press0, shear_width
+        real(c_double) :: bx0, by0, bz0, db0, in_out_ratio, dv0, drho0
+        integer(c_int) :: nmodex, nmodey, nmodez, wave_number_jet
+        real(c_double) :: jet_width, Vjet
+        real(c_double) :: B0_SB, dB_SB, R0_SB, R1_SB, H_SB, Rm_SB, Rd_SB
+    end type laps_ic
+
     type, bind(C) :: laps_diag
         real(c_double) :: time, dt, radius
         real(c_double) :: uu_ave(8), uu_rms(8), rho_u2(3)
@@ -63,6 +73,24 @@ module laps_gpu
             type(c_ptr), value :: ctx
             real(c_double), intent(in) :: uu(*)
             integer(c_int), value :: layout
+        end function
+        integer(c_int) function laps_ic_default(ic) bind(C, name='laps_ic_default')
+            import :: c_int, laps_ic
+            type(laps_ic), intent(out) :: ic
+        end function
+        integer(c_long_long) function laps_ic_nphases(ic) bind(C, name='laps_ic_nphases')
+            import :: c_long_long, laps_ic
+            type(laps_ic), intent(in) :: ic
+        end function
+        ! in place of background_fields_initialize + perturbation_initialize +
+        ! initial_calc_conserve_variable + transform_uu_real_to_fourier (mhd.f90:110-122);
+        ! phs: the phases random_number drew (times 2 pi), laps_ic_nphases of them
+        integer(c_int) function laps_init_fields(ctx, ic, phs, nphases) bind(C, name='laps_init_fields')
+            import :: c_int, c_ptr, c_double, c_long_long, laps_ic
+            type(c_ptr), value :: ctx
+            type(laps_ic), intent(in) :: ic
+            real(c_double), intent(in) :: phs(*)
+            integer(c_long_long), value :: nphases
         end function
         integer(c_int) function laps_set_time(ctx, time) bind(C, name='laps_set_time')
             import :: c_int, c_ptr, c_double

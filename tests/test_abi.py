@@ -80,3 +80,46 @@ def test_create_rejects_bad_parameters(lib, kw, code):
 def test_null_context_is_an_error(lib):
     assert lib.laps_step(None, 1, None, None, None) == ffi.LAPS_EINVAL
     assert lib.laps_wait(None, 10) == ffi.LAPS_EINVAL
+
+
+def _c_struct_fields(name):
+    txt = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "laps_gpu.h").read_text(), flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), txt, flags=re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r"^(unsigned\s+)?(long long|int|double|char)\s+", "", decl)
+        out += [re.sub(r"\[.*\]", "", v).strip() for v in decl.split(",")]
+    return out
+
+
+def _fortran_type_fields(name):
+    txt = (ROOT / "fortran" / "laps_gpu.f90").read_text()
+    body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type %s" % (name, name), txt, flags=re.S).group(1)
+    out = []
+    for line in body.splitlines():
+        if "::" in line:
+            out += [re.sub(r"\(.*\)", "", v).strip() for v in line.split("::")[1].split(",")]
+    return out
+
+
+@pytest.mark.parametrize("name,cls", [("laps_params", ffi.laps_params), ("laps_ic", ffi.laps_ic),
+                                      ("laps_diag", ffi.laps_diag)])
+def test_struct_fields_agree_across_bindings(name, cls):
+    """The header's struct, the ctypes mirror and the Fortran bind(C) type list the same
+    fields in the same order."""
+    c = _c_struct_fields(name)
+    assert [f[0] for f in cls._fields_] == c
+    assert [v.lower() for v in _fortran_type_fields(name)] == [v.lower() for v in c]
+
+
+def test_fortran_module_binds_the_stepping_entry_points():
+    txt = (ROOT / "fortran" / "laps_gpu.f90").read_text()
+    bound = set(re.findall(r"name='(laps_[a-z_0-9]+)'", txt))
+    for fn in ("laps_create", "laps_upload_state", "laps_init_fields", "laps_step", "laps_vardt", "laps_download_state",
+               "laps_diagnostics", "laps_calc_flux", "laps_calc_rhs", "laps_write_output", "laps_read_restart"):
+        assert fn in bound, fn
+    assert bound <= set(header_functions())
+    assert ctypes.sizeof(ffi.laps_ic) == 2 * 4 + 17 * 8 + 4 * 4 + 9 * 8
