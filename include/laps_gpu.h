@@ -180,6 +180,21 @@ long long laps_ic_nphases(const laps_ic* ic);
  */
 int laps_init_fields(laps_ctx* ctx, const laps_ic* ic, const double* phases, long long nphases);
 
+/*
+ * Angle statistics of the current state, the reference's offline C tool
+ * theta_ub_zpm_perp_only (data_process/3D_C/statistics.c:10-356, run per axis by
+ * pthread_theta_ub_zpm_perp_only :358-389 on an outNNN.dat): for lags l = 1 .. n_axis/2 grid
+ * spacings along `axis` (0 x, 1 y, 2 z), the angle between the components perpendicular to
+ * <B>/|<B>| of the increments of u and of B/sqrt(<rho>) ("ub"), and of z+ = u - b and
+ * z- = u + b ("zpm").  out receives 4 arrays of n_axis doubles, the contents of the four files
+ * the tool writes for the axis: ub method 1, ub method 2, zpm method 1, zpm method 2
+ * (method 1: the mean of asin(|a x b| / |a||b|) over points with both parts non-zero;
+ * method 2: asin(sum |a x b| / sum |a||b|)); elements 0 and l > n_axis/2 are 0.
+ * The means are taken over the state (the reference's mean() starts its sum uninitialised,
+ * mathlib.c:9; here it starts at 0).  Float64 on the device.
+ */
+int laps_angle_statistics(laps_ctx* ctx, int axis, double* out);
+
 /* Set the simulation time and the expanding-box radius: evolve_radius(t)
  * (AEBmod.f90:56-73,87-125), as the restart path does (mhd.f90:101-103). */
 int laps_set_time(laps_ctx* ctx, double time);

@@ -170,6 +170,11 @@ int laps_init_fields(laps_ctx* c, const laps_ic* ic, const double* phases, long 
   }
   return guarded(c, [&] { c->e->init_fields(*ic, phases); });
 }
+int laps_angle_statistics(laps_ctx* c, int axis, double* out) {
+  if (!c) return LAPS_EINVAL;
+  if (axis < 0 || axis > 2 || !out) return fail(c, LAPS_EINVAL, "axis must be 0, 1 or 2 and out non-null");
+  return guarded(c, [&] { c->e->angle_statistics(axis, out); });
+}
 int laps_set_time(laps_ctx* c, double t) { return guarded(c, [&] { c->e->set_time(t); }); }
 int laps_vardt(laps_ctx* c, double* dt) {
   return guarded(c, [&] {

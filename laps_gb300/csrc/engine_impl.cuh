@@ -16,6 +16,7 @@
 #include "launch.cuh"
 #include "diag.cuh"
 #include "ic.cuh"
+#include "stats.cuh"
 
 namespace laps {
 
@@ -113,6 +114,8 @@ class EngineBase {
   virtual void dealias_state() = 0;
   // fresh-start initial conditions generated on the device (phases of ipert 6 / 7 given)
   virtual void init_fields(const laps_ic& ic, const double* phases) = 0;
+  // perpendicular angle statistics of increments along one axis (4 arrays of n_axis)
+  virtual void angle_statistics(int axis, double* out) = 0;
 };
 
 // T: compute type of the transforms and products; TS: storage type of the state, the RK
@@ -778,6 +781,50 @@ template <class T, class TS = T> class Engine : public EngineBase {
                                                      P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     return out;
+  }
+  void angle_statistics(int axis, double* hout) override {
+    const double* rs = stage_real_state();  // 8 conserved fields, then ux, uy, uz, p
+    const Geo& g = gfull;
+    const int naxis = axis == 0 ? p.nx : (axis == 1 ? p.ny : p.nz);
+    const int nl = naxis / 2;
+    std::memset(hout, 0, 4 * (size_t)naxis * sizeof(double));
+    if (nl < 1) return;
+    double* dmean = nullptr;
+    double* dout = nullptr;
+    double* part = nullptr;
+    const int nblk = (int)std::min<long long>(4 * 152, (g.fsr + ANG_THREADS - 1) / ANG_THREADS);
+    LAPS_CK(cudaMalloc(&dmean, 4 * sizeof(double)));
+    LAPS_CK(cudaMalloc(&dout, 4 * (size_t)naxis * sizeof(double)));
+    LAPS_CK(cudaMalloc(&part, (size_t)nl * nblk * ANG_NSUM * sizeof(double)));
+    try {
+      k_state_means<TS><<<1, 32, 0, stream>>>(B.U, g.fsc, dmean);
+      LAPS_CK(cudaGetLastError());
+      double m[4];
+      LAPS_CK(cudaMemcpyAsync(m, dmean, sizeof(m), cudaMemcpyDeviceToHost, stream));
+      wait(tmo());
+      // statistics.c:86-101: b0 = <B> / |<B>|
+      const double b0abs = std::sqrt(m[1] * m[1] + m[2] * m[2] + m[3] * m[3]);
+      AngArgs a;
+      a.u = rs + 8 * g.fsr;
+      a.B = rs + 4 * g.fsr;
+      a.n = g.fsr;
+      a.nx = p.nx; a.ny = p.ny; a.nz = p.nz; a.axis = axis; a.lag0 = 1;
+      a.sqrt_rho0 = std::sqrt(m[0]);
+      a.b0x = m[1] / b0abs; a.b0y = m[2] / b0abs; a.b0z = m[3] / b0abs;
+      LAPS_CK(cudaMemsetAsync(dout, 0, 4 * (size_t)naxis * sizeof(double), stream));
+      k_angle_partial<<<dim3(nblk, nl), ANG_THREADS, 0, stream>>>(a, part);
+      LAPS_CK(cudaGetLastError());
+      k_angle_final<<<(nl + 127) / 128, 128, 0, stream>>>(part, nblk, nl, 1, naxis, dout);
+      LAPS_CK(cudaGetLastError());
+      LAPS_CK(cudaMemcpyAsync(hout, dout, 4 * (size_t)naxis * sizeof(double), cudaMemcpyDeviceToHost, stream));
+      wait(tmo());
+    } catch (...) {
+      cudaFree(dmean); cudaFree(dout); cudaFree(part);
+      throw;
+    }
+    LAPS_CK(cudaFree(dmean));
+    LAPS_CK(cudaFree(dout));
+    LAPS_CK(cudaFree(part));
   }
   const laps_params& params() const override { return p; }
   long long grid_points() const override { return gfull.fsr; }

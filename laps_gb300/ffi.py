@@ -122,6 +122,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_ic_default": (C.c_int, [P(laps_ic)]),
         "laps_ic_nphases": (C.c_longlong, [P(laps_ic)]),
         "laps_init_fields": (C.c_int, [vp, P(laps_ic), dp, C.c_longlong]),
+        "laps_angle_statistics": (C.c_int, [vp, C.c_int, dp]),
         "laps_set_time": (C.c_int, [vp, C.c_double]),
         "laps_vardt": (C.c_int, [vp, dp]),
         "laps_step": (C.c_int, [vp, C.c_int, dp, dp, P(C.c_int)]),
@@ -231,6 +232,14 @@ class Laps:
             self._ck(self.lib.laps_init_fields(self.h, C.byref(ic), _dptr(a), int(a.size)))
         else:
             self._ck(self.lib.laps_init_fields(self.h, C.byref(ic), None, 0))
+
+    def angle_statistics(self, axis: int) -> np.ndarray:
+        """Perpendicular angle statistics of the increments along ``axis`` (0 x, 1 y, 2 z):
+        rows ub method 1, ub method 2, zpm method 1, zpm method 2; column l = lag l."""
+        n = (self.p.nx, self.p.ny, self.p.nz)[axis]
+        out = np.zeros((4, n))
+        self._ck(self.lib.laps_angle_statistics(self.h, int(axis), _dptr(out)))
+        return out
 
     def set_time(self, t: float):
         self._ck(self.lib.laps_set_time(self.h, float(t)))

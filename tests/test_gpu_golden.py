@@ -1,4 +1,4 @@
-"""GPU runs of the committed golden cases (tests/golden/*.npz, made by make_golden.py from
+"""GPU runs of the committed golden cases (tests/golden/c*.npz, made by make_golden.py from
 the oracle) through the C-ABI: every field within 1e-11 relative L2, time within 1e-12."""
 from pathlib import Path
 
@@ -12,7 +12,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 @pytest.mark.parametrize("prec", [ffi.PREC_FP64, ffi.PREC_DD], ids=["fp64", "dd"])
-@pytest.mark.parametrize("path", sorted(GOLDEN.glob("*.npz")), ids=lambda p: p.stem)
+@pytest.mark.parametrize("path", sorted(GOLDEN.glob("c*.npz")), ids=lambda p: p.stem)
 def test_golden_case(path, prec):
     g = np.load(path)
     nx, ny, nz = (int(v) for v in g["shape"])
