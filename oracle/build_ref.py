@@ -62,9 +62,17 @@ def run_angle_statistics(prim, axis: int, nt: int = 0):
     with tempfile.TemporaryDirectory() as d:
         os.makedirs(os.path.join(d, "output"))
         os.chdir(d)
+        libc = ctypes.CDLL(None)
+        saved = os.dup(1)
+        log = os.open(os.path.join(d, "tool.log"), os.O_WRONLY | os.O_CREAT)
+        os.dup2(log, 1)  # the tool reports its progress on stdout
         try:
             f(uu.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nt, 1, nx, ny, nz, nvar, axis)
         finally:
+            libc.fflush(None)
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(log)
             os.chdir(cwd)
         out = []
         for kind in ("ub", "zpm"):
