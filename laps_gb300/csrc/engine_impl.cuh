@@ -156,6 +156,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
   // each map is that geometry's KeptCopies box, which the kernel recomputes from its Geo.
   CUtensorMap tm_a[2]{}, tm_b[2]{};
   int box_a[2]{}, box_b[2]{};
+  // pass E: the W2 map, then the state U and the RK register R in kept-kz boxes (L2 prefetch)
+  CUtensorMap tm_e3[2][3]{};
+  int box_e[2]{};
   int npart = 0;
 
   template <class X> X* dalloc(size_t n) {
@@ -293,6 +296,10 @@ template <class T, class TS = T> class Engine : public EngineBase {
         box_b[i] = KeptCopies(gk.ky_lo, gk.ky_hi, q.ny, tile_gran((int)sizeof(C))).box;
         tm_a[i] = work_tensor_map(B.U, g, 8, (int)(sizeof(CS) / 8), 1, box_a[i]);
         tm_b[i] = work_tensor_map(B.W1, g, 19, ew, box_b[i], 1);
+        box_e[i] = KeptCopies(gk.kz_lo, gk.kz_hi, q.nz, 1).box;
+        tm_e3[i][0] = tm_e;
+        tm_e3[i][1] = work_tensor_map(B.U, g, 8, (int)(sizeof(CS) / 8), 1, box_e[i]);
+        tm_e3[i][2] = work_tensor_map(B.R, g, 8, ew, 1, box_e[i]);
       }
     }
     LAPS_CK(cudaMemsetAsync(B.U, 0, 8 * g.fsc * sizeof(CS), stream));
@@ -455,7 +462,12 @@ template <class T, class TS = T> class Engine : public EngineBase {
   void passD(const PassArgs& a) { launch_passD<T, TS>(stream, p.ny, B, a, passk(), twy, &tm_d); }
   void passE(const PassArgs& a) {
     if (P.variant == LAPS_VARIANT_3DI) launch_passE3i<T, TS>(stream, p.nz, B, a, passk(), twz, nullptr);
-    else launch_passE<T, TS>(stream, p.nz, B, a, passk(), twz, &tm_e);
+    else {
+      const int want = KeptCopies(a.g.kz_lo, a.g.kz_hi, p.nz, 1).box;
+      const int i = box_e[1] == want ? 1 : 0;
+      if (box_e[i] != want) throw Error{LAPS_EINVAL, "no tile map for this geometry"};
+      launch_passE<T, TS>(stream, p.nz, B, a, passk(), twz, tm_e3[i]);
+    }
   }
 
   // geometry of the inverse side (A-C) and of the forward side (D-E) of a stage

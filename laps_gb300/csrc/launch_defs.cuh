@@ -108,7 +108,7 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
       a0.e_first = 1;                                                                                                   \
       grid.z = 7;                                                                                                       \
     }                                                                                                                   \
-    k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw, *tm);                                     \
+    k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw, tm[0], tm[1], tm[2]);                                     \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passE, k_passE, nky)

@@ -51,6 +51,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// 3-D tile prefetch global -> L2 (no shared memory, no completion to wait for): a hint that
+// brings a tile the block will read with ordinary loads later into L2 ahead of use
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+
 // Column tile loader of one block: up to two input buffers (two mbarriers, one per buffer;
 // a buffer reused for a later input waits on the barrier's next phase).
 struct TileLoad {
