@@ -392,9 +392,12 @@ def run_ours(args):
         host_prim = np.empty((4,) + prim.shape[1:])
         pinned = False
     e2e_ctx = ffi.Laps(p)
-    e2e_ctx.upload_state(host_in, primitive=True)  # warm the path once
+    e2e_ctx.upload_state(host_in, primitive=True)  # warm the path once: upload, steps, download
     e2e_ctx.set_time(0.0)
     e2e_ctx.step(2)
+    rc = lib.laps_download_state(e2e_ctx.h, host_out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                 host_prim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == 0
     barrier(ws)
     t0 = time.perf_counter()
     e2e_ctx.upload_state(host_in, primitive=True)

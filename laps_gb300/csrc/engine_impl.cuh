@@ -373,6 +373,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
     if (graph_steady) cudaGraphExecDestroy(graph_steady);
     for (void* a : allocs) cudaFree(a);
     if (h_st) cudaFreeHost(h_st);
+    for (cudaEvent_t e : fev)
+      if (e) cudaEventDestroy(e);
+    if (cstream) cudaStreamDestroy(cstream);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -582,14 +585,49 @@ template <class T, class TS = T> class Engine : public EngineBase {
   }
 
   // ---------------------------------------------------------------- API
+  // copies between the host and the device run on their own stream, field by field, so that
+  // the transforms of the fields that have arrived (upload) or are done (download) overlap them
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t fev[13] = {};
+  void copy_stream_ready() {
+    if (cstream) return;
+    LAPS_CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
+    for (auto& e : fev) LAPS_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // one real field -> its spectrum through the intermediate tmp (one spectral field)
+  void forward_one(const SRS* real, CS* out, CS* tmp) {
+    const Geo& g = gfull;
+    rows_r2c(real, tmp, (long long)g.ny * g.nz);
+    col_plain(tmp, tmp, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twys);
+    col_plain(tmp, out, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twzs);
+  }
+  void inverse_one(const CS* spec, SRS* real, CS* tmp) {
+    const Geo& g = gfull;
+    col_plain(spec, tmp, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twzs);
+    col_plain(tmp, tmp, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twys);
+    rows_c2r(tmp, real, (long long)g.ny * g.nz);
+  }
+
   void upload(const double* h, int layout) override {
     const Geo& g = gfull;
-    double* stage = (double*)B.W2;  // 8 real float64 fields fit in 15 complex fields
-    LAPS_CK(cudaMemcpyAsync(stage, h, 8 * g.fsr * sizeof(double), cudaMemcpyHostToDevice, stream));
-    k_upload_convert<TS><<<1024, 256, 0, stream>>>(stage, (SRS*)B.W1, g.fsr, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma,
+    copy_stream_ready();
+    // the 8 float64 fields land in W2; the per-field transform works through the 9th
+    // spectral field of W2, after them (8 fsr doubles <= 8 fsc state-type complexes)
+    double* stage = (double*)B.W2;
+    CS* tmp = W2s() + 8 * g.fsc;
+    for (int f = 0; f < 8; f++) {
+      LAPS_CK(cudaMemcpyAsync(stage + f * g.fsr, h + f * g.fsr, g.fsr * sizeof(double), cudaMemcpyHostToDevice, cstream));
+      LAPS_CK(cudaEventRecord(fev[f], cstream));
+    }
+    // field f needs fields <= f (rho for the momentum, all for the energy): convert and
+    // transform each as soon as it is in
+    for (int f = 0; f < 8; f++) {
+      LAPS_CK(cudaStreamWaitEvent(stream, fev[f], 0));
+      k_upload_field<TS><<<1024, 256, 0, stream>>>(stage, (SRS*)B.W1, g.fsr, f, layout == LAPS_LAYOUT_PRIMITIVE, P.gamma,
                                                    P.variant == LAPS_VARIANT_3DI);
-    LAPS_CK(cudaGetLastError());
-    forward3d((const SRS*)B.W1, B.U, 8);
+      LAPS_CK(cudaGetLastError());
+      forward_one((const SRS*)B.W1 + f * g.fsr, B.U + f * g.fsc, tmp);
+    }
     // mhd.f90:135: dt = 0 before the first vardt, so the first CFL value is taken as is
     LAPS_CK(cudaMemsetAsync(&st->dt, 0, sizeof(double), stream));
     dealiased = false;
@@ -844,13 +882,31 @@ template <class T, class TS = T> class Engine : public EngineBase {
   void download(double* uu, double* prim) override {
     if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
     const Geo& g = gfull;
-    inverse3d(B.U, 8);
+    copy_stream_ready();
     double* out = (double*)B.W2;  // 12 real float64 fields fit in 15 complex fields
-    k_download_convert<TS><<<1024, 256, 0, stream>>>((const SRS*)B.W1, uu ? out : nullptr, prim ? out + 8 * g.fsr : nullptr,
-                                                     g.fsr, P.gamma, P.variant == LAPS_VARIANT_3DI);
-    LAPS_CK(cudaGetLastError());
-    if (uu) LAPS_CK(cudaMemcpyAsync(uu, out, 8 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
-    if (prim) LAPS_CK(cudaMemcpyAsync(prim, out + 8 * g.fsr, 4 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    // the per-field inverse works through one spectral field of W1 after the 8 real fields
+    SRS* real = (SRS*)B.W1;
+    CS* tmp = (CS*)((unsigned char*)B.W1 + (8 * g.fsr * (long long)sizeof(SRS) + 255) / 256 * 256);
+    for (int f = 0; f < 8; f++) {
+      inverse_one(B.U + f * g.fsc, real + f * g.fsr, tmp);
+      if (uu) {  // conserved field f: convert, then copy while the next field transforms
+        k_field_to_double<TS><<<1024, 256, 0, stream>>>(real + f * g.fsr, out + f * g.fsr, g.fsr);
+        LAPS_CK(cudaGetLastError());
+        LAPS_CK(cudaEventRecord(fev[f], stream));
+        LAPS_CK(cudaStreamWaitEvent(cstream, fev[f], 0));
+        LAPS_CK(cudaMemcpyAsync(uu + f * g.fsr, out + f * g.fsr, g.fsr * sizeof(double), cudaMemcpyDeviceToHost, cstream));
+      }
+    }
+    if (prim) {  // the primitives need every field
+      k_download_convert<TS><<<1024, 256, 0, stream>>>((const SRS*)real, nullptr, out + 8 * g.fsr, g.fsr, P.gamma,
+                                                       P.variant == LAPS_VARIANT_3DI);
+      LAPS_CK(cudaGetLastError());
+      LAPS_CK(cudaEventRecord(fev[8], stream));
+      LAPS_CK(cudaStreamWaitEvent(cstream, fev[8], 0));
+      LAPS_CK(cudaMemcpyAsync(prim, out + 8 * g.fsr, 4 * g.fsr * sizeof(double), cudaMemcpyDeviceToHost, cstream));
+    }
+    LAPS_CK(cudaEventRecord(fev[12], cstream));
+    LAPS_CK(cudaStreamWaitEvent(stream, fev[12], 0));
     wait(tmo());
   }
   void download_spectral(double* uf) override {

@@ -288,6 +288,33 @@ __global__ void k_upload_convert(const double* __restrict__ h, typename Store<T>
   }
 }
 
+// one field f of the conversion above, for the pipelined upload (the fields it reads - rho
+// for the momentum, all eight for the energy - have arrived)
+template <class T>
+__global__ void k_upload_field(const double* __restrict__ h, typename Store<T>::R* __restrict__ u, long long n, int f,
+                               int primitive, double gamma, int incomp) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = h[f * n + i];
+    if (primitive) {
+      if (f >= 1 && f <= 3) {
+        v = h[i] * v;
+      } else if (f == 7 && !incomp) {
+        const double rho = h[i], ux = h[n + i], uy = h[2 * n + i], uz = h[3 * n + i];
+        const double bx = h[4 * n + i], by = h[5 * n + i], bz = h[6 * n + i];
+        v = v / (gamma - 1) + 0.5 * (rho * (ux * ux + uy * uy + uz * uz) + bx * bx + by * by + bz * bz);
+      }
+    }
+    Store<T>::st(u + f * n + i, Real<T>::from_d(v));
+  }
+}
+
+// real T field -> float64 (the conserved fields of the pipelined download)
+template <class T>
+__global__ void k_field_to_double(const typename Store<T>::R* __restrict__ u, double* __restrict__ h, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    h[i] = Real<T>::to_d(Store<T>::ld(u + i));
+}
+
 // conserved T -> conserved doubles + primitives (ux, uy, uz, p); mhdrhs.f90:282-294
 template <class T>
 __global__ void k_download_convert(const typename Store<T>::R* __restrict__ u, double* __restrict__ h, double* __restrict__ hp,
