@@ -30,6 +30,11 @@ template <class T, int N> struct Col {
   static constexpr int SMEM = NTILE * N * TX * (int)sizeof(C);  // one buffer per tile
 };
 
+// Two column tiles of length N no longer fit one block's shared memory (1024-point columns of
+// 16-byte elements: 2 x 128 KB): such passes keep one tile in shared memory and the other
+// thread's-own elements in registers
+template <class T, int N> __host__ __device__ constexpr bool col_one_buffer() { return 2 * Col<T, N>::SMEM > 220 * 1024; }
+
 // T: the compute type of the transforms and products; TS: the storage type of the state
 // and of the RK register (the same except in the FP32-transform mode, where TS is
 // float-float)

@@ -78,10 +78,14 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passB<T, TS, NN>, 2 * CL::SMEM);                                                                         \
+    /* 2-D: one buffer per tile (the state is read by the threads) - tiles are laid out with */                      \
+    /* two buffers each, so only a single-tile block may drop the second; 3-D: the two inputs  */                      \
+    const int smB = (a.P.two_d && CL::NTILE == 1) ? CL::SMEM : 2 * CL::SMEM;                                            \
+    if (!a.P.two_d && col_one_buffer<T, NN>()) throw Error{LAPS_EINVAL, "column tiles exceed shared memory"};             \
+    set_smem(k_passB<T, TS, NN>, smB);                                                                                  \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
-    k_passB<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw, *tm);                                 \
+    k_passB<T, TS, NN><<<grid, CL::THREADS, smB, stream>>>(B, a, kk, tw, *tm);                                          \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passB, k_passB, nz)
@@ -89,9 +93,10 @@ LAPS_COL_PASS(launch_passB, k_passB, nz)
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    set_smem(k_passD<T, TS, NN>, 2 * CL::SMEM);                                                                             \
+    const int smD = col_one_buffer<T, NN>() ? CL::SMEM : 2 * CL::SMEM;                                                  \
+    set_smem(k_passD<T, TS, NN>, smD);                                                                                  \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE, a.P.variant == LAPS_VARIANT_3DI ? 5 : (a.mass_from_state ? 6 : 8)); \
-    k_passD<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a, kk, tw, *tm);                                       \
+    k_passD<T, TS, NN><<<grid, CL::THREADS, smD, stream>>>(B, a, kk, tw, *tm);                                          \
     break;                                                                                                              \
   }
 LAPS_COL_PASS(launch_passD, k_passD, nz)

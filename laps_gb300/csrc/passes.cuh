@@ -462,6 +462,12 @@ constexpr unsigned c_fused = 0x7FFFFu & ~((1u << 6) | (1u << 9) | (1u << 10));
 // Rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
 // (Hall) in one batch; when two rows of 19 line slots do not fit in shared memory (1024-point
 // rows of 16-byte elements) a block takes one row and batches of 12 lines.
+// Lines per batch of the 512- and 1024-point rows: 16 (256 / 512 threads) leaves 128 or more
+// registers per thread (24 spilled: 3-D incompressible 512^3 pass C 22.7 -> 18.3 ms per step);
+// LAPS_PASSC_LB_LONG overrides it at build time for tuning sweeps.
+#ifndef LAPS_PASSC_LB_LONG
+#define LAPS_PASSC_LB_LONG 16
+#endif
 template <int NX, int CB> struct PassCCfg {
   static constexpr int H = NX / 2;
   static constexpr int TPL = Plan<H>::TPL;
@@ -469,7 +475,7 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int NF = 19;             // line slots per row
   static constexpr int LC = RowLen<H>::V;   // padded complex per line
   static constexpr bool ONE_ROW = 2 * MUL * NF * LC * CB > 200 * 1024;
-  static constexpr int LB = ONE_ROW ? 12 : 24 * MUL;  // lines per batch
+  static constexpr int LB = ONE_ROW ? 12 : (NX >= 512 ? LAPS_PASSC_LB_LONG : 24 * MUL);  // lines per batch
   static constexpr int THREADS = LB * TPL;
   static constexpr int ROWS = ONE_ROW ? 1 : 2 * MUL;
   // Paired rows: rows 2p and 2p+1 of a field share one complex line of NX points,
@@ -724,6 +730,13 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
 template <class T> struct ColOcc {
   static constexpr int V = sizeof(typename Store<T>::C) == 8 ? LAPS_MINB_COL : (std::is_same<T, double>::value ? 3 : 4);
 };
+// the same registers per thread for longer columns, whose blocks have more threads (512- and
+// 1024-point columns: 256 and 512 threads; a fixed block count would leave 32-64 registers
+// and spill)
+template <class T, int N> struct ColOccN {
+  static constexpr int W = ColOcc<T>::V * 128 / Col<T, N>::THREADS;
+  static constexpr int V = W < 1 ? 1 : W;
+};
 
 // ============================================================================ pass D
 // forward y-FFT of the fluxes with the kx, ky parts of the spectral right-hand side folded
@@ -754,7 +767,7 @@ __constant__ DGroup c_dgroups[2][8] = {
      {{5, -1, -1}, DG_EZ, 6}}};
 
 template <class T, class TS, int NY>
-__global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V)
+__global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOccN<T, NY>::V)
     k_passD(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy,
             const __grid_constant__ CUtensorMap tmap) {
   const PT<T>& pc = kk.pc;
@@ -794,22 +807,51 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V)
     }
   };
   constexpr bool PAIR = sizeof(C) == 8;
+  // one shared-memory tile (1024-point columns of 16-byte elements): the inputs come one
+  // after the other into buffer 0, and the tile a later input would have found in the other
+  // buffer is kept as each thread's own elements in registers (rb)
+  constexpr bool ONEBUF = col_one_buffer<T, NY>();
+  static_assert(!ONEBUF || CL::NTILE == 1, "one buffer: single-tile blocks (ColCtx lays tiles out with two buffers)");
+  cx<T> rb[2][ONEBUF ? CL::EPT : 1];
+  auto vget = [&](int vb, int cur, int m) -> cx<T> {
+    if constexpr (ONEBUF) return vb == cur ? Store<T>::ldc(x.at(0, m)) : rb[vb][m];
+    else return Store<T>::ldc(x.at(vb, m));
+  };
+  auto vput0 = [&](int cur, int m, cx<T> v) {
+    if constexpr (ONEBUF) {
+      if (cur == 0) Store<T>::stc(x.at(0, m), v);
+      else rb[0][m] = v;
+    } else {
+      Store<T>::stc(x.at(0, m), v);
+    }
+  };
   issue(0, 0);
-  if (nin > 1) issue(1, 1);
+  if (nin > 1 && !ONEBUF) issue(1, 1);
   if (PAIR) {
     if (!tl.wait(0, a.st) || (nin > 1 && !tl.wait(1, a.st))) return;
     fft_lines_pair<T, NY, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twy, 1);
   }
 #pragma unroll 1
   for (int k = 0; k < nin; k++) {
+    int cur = 0;  // the (virtual) buffer input k is in
     if (k == 2 || !PAIR) {
       const int bi = k == 1 || (k == 2 && kind == DG_Q8) ? 1 : 0;
-      if (k == 2) {  // the buffer's earlier contents were read and written by the threads
-        if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(2, bi);
+      cur = bi;
+      if constexpr (ONEBUF) {
+        if (k > 0) {  // buffer 0's earlier contents were read by the threads
+          if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue(k, 0);
+        }
+        if (!tl.wait(0, a.st)) return;
+        fft_lines<T, NY, -1, TX, 1>(x.buf(0), x.c, x.t, true, twy, 1);
+      } else {
+        if (k == 2) {  // the buffer's earlier contents were read and written by the threads
+          if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue(2, bi);
+        }
+        if (!tl.wait(bi, a.st)) return;
+        fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
       }
-      if (!tl.wait(bi, a.st)) return;
-      fft_lines<T, NY, -1, TX, 1>(x.buf(bi), x.c, x.t, true, twy, 1);
     }
     if (ok) {
 #pragma unroll 2
@@ -819,11 +861,11 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V)
         kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
         const bool st_ok = g.ky_in(ky);
         C* o = ob + (long long)ky * g.kxp;
-        cx<T> v0 = Store<T>::ldc(x.at(0, m)), v1 = cx_zero<T>();
-        if (k > 0) v1 = Store<T>::ldc(x.at(1, m));
+        cx<T> v0 = vget(0, cur, m), v1 = cx_zero<T>();
+        if (k > 0) v1 = vget(1, cur, m);
         if (kind == DG_Q8) {
           if (k == 1) {  // fold the two fluxes into buffer 0, unscaled
-            Store<T>::stc(x.at(0, m), -(mul_i(v0, ax) + mul_i(v1, ay)));
+            vput0(cur, m, -(mul_i(v0, ax) + mul_i(v1, ay)));
             if (nin == 2 && st_ok) {
               cx<T> q = -(mul_i(v0, ax) + mul_i(v1, ay));
               Store<T>::stc(o, {Real<T>::mul_pow2(q.re, sexp), Real<T>::mul_pow2(q.im, sexp)});
@@ -863,6 +905,10 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOcc<T>::V)
             } else Store<T>::stc(o + 4 * g.fsc, v0);
             break;
         }
+      }
+      if constexpr (ONEBUF) {  // keep this input's transform before the next one overwrites it
+#pragma unroll
+        for (int m = 0; m < CL::EPT; m++) rb[cur][m] = Store<T>::ldc(x.at(0, m));
       }
     }
     __syncthreads();
@@ -983,7 +1029,7 @@ __device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& p
 // the time advance of variable v = blockIdx.z.  Tile: kx0..kx0+7, one kept ky row; reads all
 // z of W2, writes kept kz of U (and R).
 template <class T, class TS, int NZ>
-__global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOcc<T>::V)
+__global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
     k_passE(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twz,
             const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmu,
             const __grid_constant__ CUtensorMap tmr) {

@@ -131,3 +131,22 @@ def test_2d_alfven_wave(prec):
     x = np.arange(n) * (2 * math.pi / n)
     dec = math.exp(-eta * t)
     assert np.abs(uu[6] + 0.1 * np.sin(x - t) * dec).max() < 1e-5
+
+
+@pytest.mark.parametrize("prec", PRECS + [ffi.PREC_FP32], ids=PREC_ID + ["fp32"])
+@pytest.mark.parametrize("shape", [(32, 1024), (1024, 16)], ids=["ny1024", "nx1024"])
+def test_2d_long_lines(prec, shape):
+    """1024-point lines: 2-D y columns of 16-byte elements keep one tile in shared memory (the
+    second in registers), 1024-point x rows run one row per block."""
+    kw = D_CASES["hall"]
+    prim = turbulence_ic((shape[0], shape[1], 1), seed=15, kmax=6, rms_u=0.3, rms_b=0.3)
+    o, g = start_2d(shape, kw, prim, prec)
+    o.dt = 0.0
+    for _ in range(3):
+        o.step()
+    t, dt, st = g.step(3)
+    assert st == 0
+    tol = 1e-5 if prec == ffi.PREC_FP32 else 1e-11
+    assert abs(dt - o.dt) <= tol * o.dt
+    uu, _ = g.download_state()
+    assert rel_l2(uu, o.uu, state_floor(o.uu)).max() < tol
