@@ -206,6 +206,36 @@ __device__ __forceinline__ void fft_lines(typename Store<T>::C* s, int l, int t,
   }
 }
 
+// Forward transform of one warp-local row of N points as a real call (not inlined), so that
+// callers transforming in both directions carry one copy of the butterflies: the backward
+// transform is conj(forward(conj(x))).  For float-float rows, whose code otherwise outgrows the
+// instruction cache (the x pass stalled on instruction fetch first).
+template <class T, int N>
+__device__ __noinline__ void fft_row_fwd_call(typename Store<T>::C* z, int t, bool active,
+                                              const typename Store<T>::C* __restrict__ tw, int twstep) {
+  fft_lines<T, N, -1, 1, 0, true>(z, 0, t, active, tw, twstep);
+}
+// Conjugate the elements t + 16 i (i < 16) of a 256-point row: the elements thread t loads
+// first and stores last in fft_lines (two radix-16 stages), so no barrier is needed around it
+template <class T>
+__device__ __forceinline__ void row256_conj(typename Store<T>::C* z, int t, bool active) {
+  if (!active) return;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    typename Store<T>::C* p = z + sm_idx<1>(t + 16 * i);
+    cx<T> v = Store<T>::ldc(p);
+    Store<T>::stc(p, cx<T>{v.re, -v.im});
+  }
+}
+template <class T, int N, int DIR>
+__device__ __forceinline__ void fft_row_shared(typename Store<T>::C* z, int t, bool active,
+                                               const typename Store<T>::C* __restrict__ tw, int twstep) {
+  static_assert(N == 256, "the conjugation pattern is that of two radix-16 stages");
+  if (DIR > 0) row256_conj<T>(z, t, active);
+  fft_row_fwd_call<T, N>(z, t, active, tw, twstep);
+  if (DIR > 0) row256_conj<T>(z, t, active);
+}
+
 // Two tiles transformed together (column passes with two inputs): one pass over the stages,
 // the same twiddles applied to both, half the barriers.  FP32 lines only (two 16-element
 // sets of float-float or FP64 values would not fit the register budget); other types

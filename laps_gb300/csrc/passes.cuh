@@ -522,6 +522,10 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     else return sr + 2 * rr * CF::NF * CF::LC + row_real_idx(x);
   };
   const int kk_in = g.kx_keep;
+  // float-float 256-point rows: one (called) copy of the transform for both directions (pass
+  // time -9 %: the kernel stalled on instruction fetch; FP64 rows, ALU-bound, lose 3 % and
+  // keep both inlined copies)
+  constexpr bool SHARED_FFT = std::is_same<T, dd>::value && NX == 256 && CF::PAIRED;
   if constexpr (CF::PAIRED) {
     // ---- inverse x-transform of row pairs: Z = X_a + i X_b over the full line (the
     // imaginary parts of the DC and Nyquist terms are dropped, as the reference's c2r does)
@@ -537,7 +541,8 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
         pair_c2r<T, NX>(z, ltp, kk_in, xa, xa + g.kxp);
       }
       __syncwarp();  // a line and its threads stay within one warp until the physics
-      fft_lines<T, NX, +1, 1, 0, true>(z, 0, ltp, act, twx, 1);
+      if constexpr (SHARED_FFT) fft_row_shared<T, NX, +1>(z, ltp, act, twx, 1);
+      else fft_lines<T, NX, +1, 1, 0, true>(z, 0, ltp, act, twx, 1);
     }
   } else {
     // ---- c2r of the inputs, one half-length complex line per row
@@ -698,7 +703,8 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       const bool act = L < NPAIR * nfl;
       const int pr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
       C* z = sc + (pr * CF::NF + f) * CF::LCP;
-      fft_lines<T, NX, -1, 1, 0, true>(z, 0, ltp, act, twx, 1);
+      if constexpr (SHARED_FFT) fft_row_shared<T, NX, -1>(z, ltp, act, twx, 1);
+      else fft_lines<T, NX, -1, 1, 0, true>(z, 0, ltp, act, twx, 1);
       if (act) {
         C* xa = b.W1 + f * g.fsc + (row0 + 2 * pr) * g.kxp;
         pair_r2c<T, NX>(z, ltp, kk_in, xa, xa + g.kxp, sexp);
