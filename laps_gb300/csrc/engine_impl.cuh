@@ -281,6 +281,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     }
 
     LAPS_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    side_ready();  // before any capture of the step
     B.U = dalloc<CS>(8 * g.fsc);
     B.R = dalloc<C>(8 * g.fsc);
     B.W1 = (C*)dalloc<unsigned char>(19 * g.fsc * WE);
@@ -376,6 +377,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
     for (cudaEvent_t e : fev)
       if (e) cudaEventDestroy(e);
     if (cstream) cudaStreamDestroy(cstream);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -447,6 +451,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.mass_from_state = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
     a.e_first = 0;
     a.rhs_only = rhs_mode;
+    a.mass_done = 0;
     return a;
   }
   // the map whose box matches the kept-row copies the kernel makes for a.g
@@ -500,8 +505,22 @@ template <class T, class TS = T> class Engine : public EngineBase {
     PassArgs ao = args(g_out(), stage, store_rk, 0);
     // the first stage after an upload must also clear every mode outside the kept box
     if (!dealiased) ao.g = gfull;
+    // the continuity update reads and writes only the state and RK register, which pass D
+    // does not touch: it runs on a side stream beside pass D, joined before pass E
+    const bool fork = ao.mass_from_state && !ao.rhs_only && P.variant != LAPS_VARIANT_3DI;
+    if (fork) {
+      side_ready();
+      LAPS_CK(cudaEventRecord(ev_fork, stream));
+      LAPS_CK(cudaStreamWaitEvent(side, ev_fork, 0));
+      launch_mass_rk<T, TS>(side, B, ao, passk());
+      LAPS_CK(cudaEventRecord(ev_join, side));
+    }
     passD(ao);
     mark(3);
+    if (fork) {
+      LAPS_CK(cudaStreamWaitEvent(stream, ev_join, 0));
+      ao.mass_done = 1;
+    }
     passE(ao);
     mark(4);
     dealiased = true;
@@ -589,6 +608,15 @@ template <class T, class TS = T> class Engine : public EngineBase {
   // the transforms of the fields that have arrived (upload) or are done (download) overlap them
   cudaStream_t cstream = nullptr;
   cudaEvent_t fev[13] = {};
+  // side stream of the step (the continuity update beside pass D)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  void side_ready() {
+    if (side) return;
+    LAPS_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    LAPS_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    LAPS_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  }
   void copy_stream_ready() {
     if (cstream) return;
     LAPS_CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));

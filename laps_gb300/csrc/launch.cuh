@@ -60,6 +60,7 @@ template <class T, class TS> void launch_passD(cudaStream_t stream, int N, Bufs<
                                              const CUtensorMap* tm);
 template <class T, class TS> void launch_passE(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
                                              const CUtensorMap* tm);
+template <class T, class TS> void launch_mass_rk(cudaStream_t stream, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk);
 template <class T, class TS> void launch_passE3i(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* tw,
                                              const CUtensorMap* tm);
 

@@ -23,6 +23,7 @@ struct PassArgs {
   int e_first;     // pass E: variable of blockIdx.z = 0 (the continuity update runs in a launch
                    // of its own before the momentum is overwritten)
   int rhs_only;    // store the right-hand side (fnl) in R and leave the state (laps_calc_rhs)
+  int mass_done;   // the continuity update (k_mass_rk) was launched already, beside pass D
   StepState* st;
 };
 
