@@ -464,6 +464,10 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_source": src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": pb[name]},
+        # every FFT pass: algorithmic bytes over its event-timed launch, against the same peak
+        "passes_hbm": {PASS_NAMES[i]: {"gbs": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9,
+                                       "frac": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9 / peak}
+                       for i in range(5) if pb[PASS_NAMES[i]] and pass_ms[i] > 0},
         "e2e": {"value": e2e_v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "pinned": pinned, **e2e_parts},
         "clocks": clk.summary(),
