@@ -531,7 +531,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
     enqueue_stage(2, false, false);
     k_advance_time<<<1, 32, 0, stream>>>(st, p.radius0, P.Ur, P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
-    tables();
+    // the wave-number tables follow the radius; without expansion (Ur = 0) R stays R0 and
+    // the tables built at creation / set_time stay exact (R0 / R = 1, so k^2 = (k R0 / R)^2)
+    if (P.Ur != 0.0) tables();
     mark(5);
   }
 
@@ -975,7 +977,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     // per stage: passes A (3-D), B, C, D, E (E in two launches when the continuity term comes
     // from the momentum); per step: dt finalisation, time advance, two table updates
     const bool mass = P.variant != LAPS_VARIANT_3DI && (P.dealias == 1 || P.dealias == 3);
-    i->kernels_per_step = 3 * ((P.two_d ? 4 : 5) + (mass ? 1 : 0)) + 4;
+    i->kernels_per_step = 3 * ((P.two_d ? 4 : 5) + (mass ? 1 : 0)) + 2 + (P.Ur != 0.0 ? 2 : 0);
     i->graph = graph_steady != nullptr;
   }
 };

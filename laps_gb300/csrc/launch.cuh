@@ -26,6 +26,13 @@ struct Error {
 
 // opt in to more than the default 48 KB per block; the default covers static and dynamic shared
 // memory together, so requests close to it opt in too (kernels keep < 8 KB static)
+// blocks of the continuity update: four per SM, or fewer when the kept modes are fewer
+inline int mass_rk_blocks(const Geo& g) {
+  const long long tot = (long long)g.kx_keep * g.nky() * g.nkz();
+  const long long nb = (tot + 255) / 256;
+  return (int)(nb < 4 * 152 ? (nb > 0 ? nb : 1) : 4 * 152);
+}
+
 template <class K> inline void set_smem(K kernel, int bytes) {
   if (bytes > 40 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }

@@ -109,7 +109,7 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
     PassArgs a0 = a;                                                                                                    \
     a0.e_first = 0;                                                                                                     \
     if (a.mass_from_state) { /* continuity from the momentum first, then variables 1..7 */                             \
-      if (!a.mass_done) k_mass_rk<T, TS><<<4 * 152, 256, 0, stream>>>(B, a, kk);                                        \
+      if (!a.mass_done) k_mass_rk<T, TS><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk);                             \
       a0.e_first = 1;                                                                                                   \
       grid.z = 7;                                                                                                       \
     }                                                                                                                   \
@@ -150,7 +150,7 @@ void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK
 // the continuity update alone (forked beside pass D by the step)
 template <class T, class TS>
 void launch_mass_rk(cudaStream_t stream, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk) {
-  k_mass_rk<T, TS><<<4 * 152, 256, 0, stream>>>(B, a, kk);
+  k_mass_rk<T, TS><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk);
   LAPS_CK(cudaGetLastError());
 }
 
