@@ -123,3 +123,26 @@ def test_fortran_module_binds_the_stepping_entry_points():
         assert fn in bound, fn
     assert bound <= set(header_functions())
     assert ctypes.sizeof(ffi.laps_ic) == 2 * 4 + 17 * 8 + 4 * 4 + 9 * 8
+
+
+def test_ic_defaults_and_phase_counts(lib):
+    """laps_ic_default holds the reference's initialisers and laps_ic_nphases the phase counts
+    of the random-phase cases, as the oracle states them (no device needed)."""
+    from oracle import ic as oic
+
+    ic = ffi.ic_params()
+    ref = oic.ic_default()
+    for name, _ in ffi.laps_ic._fields_:
+        assert getattr(ic, name) == ref[name], name
+    for ipert in (0, 1, 6, 7, 8):
+        for m in ((1, 0, 0), (3, 2, 1), (16, 16, 16)):
+            kw = dict(ipert=ipert, nmodex=m[0], nmodey=m[1], nmodez=m[2])
+            d = dict(ref, **kw)
+            assert lib.laps_ic_nphases(ctypes.byref(ffi.ic_params(**kw))) == oic.nphases(d)
+    assert lib.laps_ic_nphases(None) == 0
+
+
+def test_post_processing_calls_need_a_context(lib):
+    ic = ffi.ic_params(ifield=3)
+    assert lib.laps_init_fields(None, ctypes.byref(ic), None, 0) == ffi.LAPS_EINVAL
+    assert lib.laps_angle_statistics(None, 0, None) == ffi.LAPS_EINVAL
