@@ -481,9 +481,11 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int ROWS = ONE_ROW ? 1 : 2 * MUL;
   // Paired rows: rows 2p and 2p+1 of a field share one complex line of NX points,
   // z = x_2p + i x_2p+1, so a row pair takes one full-length complex FFT and no twiddled
-  // packing; lines of more than one warp (NX = 1024) keep the half-length form.
+  // packing; 1024-point lines (two warps) pair too, with block barriers, while one-row blocks
+  // (1024-point rows of 16-byte types) keep the half-length form.
   static constexpr int TPLP = Plan<NX>::TPL;
-  static constexpr bool PAIRED = !ONE_ROW && TPLP <= 32;
+  static constexpr bool PAIRED = !ONE_ROW && TPLP <= 64;
+  static constexpr bool LWARP = TPLP <= 32;  // a paired line within one warp (else two: block barriers)
   static constexpr int LCP = RowLen<NX>::V;   // padded complex per paired line
   static constexpr int LBP = THREADS / TPLP;  // paired lines per batch
   static constexpr int FSTR = PAIRED ? 2 * LCP : 2 * LC;  // field stride in reals
@@ -541,9 +543,12 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
         const C* xa = b.W2 + f * g.fsc + (row0 + 2 * pr) * g.kxp;
         pair_c2r<T, NX>(z, ltp, kk_in, xa, xa + g.kxp);
       }
-      __syncwarp();  // a line and its threads stay within one warp until the physics
+      // a line and its threads stay within one warp until the physics (1024-point lines: two
+      // warps, synchronised by block barriers every thread of the block reaches)
+      if constexpr (CF::LWARP) __syncwarp();
+      else __syncthreads();
       if constexpr (SHARED_FFT) fft_row_shared<T, NX, +1>(z, ltp, act, twx, 1);
-      else fft_lines<T, NX, +1, 1, 0, true>(z, 0, ltp, act, twx, 1);
+      else fft_lines<T, NX, +1, 1, 0, CF::LWARP>(z, 0, ltp, act, twx, 1);
     }
   } else {
     // ---- c2r of the inputs, one half-length complex line per row
@@ -705,7 +710,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       const int pr = act ? L / nfl : 0, f = act ? flist[L % nfl] : 0;
       C* z = sc + (pr * CF::NF + f) * CF::LCP;
       if constexpr (SHARED_FFT) fft_row_shared<T, NX, -1>(z, ltp, act, twx, 1);
-      else fft_lines<T, NX, -1, 1, 0, true>(z, 0, ltp, act, twx, 1);
+      else fft_lines<T, NX, -1, 1, 0, CF::LWARP>(z, 0, ltp, act, twx, 1);
       if (act) {
         C* xa = b.W1 + f * g.fsc + (row0 + 2 * pr) * g.kxp;
         pair_r2c<T, NX>(z, ltp, kk_in, xa, xa + g.kxp, sexp);
