@@ -78,6 +78,15 @@ inline CUtensorMap work_tensor_map(void* base, const Geo& g, int nfields, int ew
   return m;
 }
 
+// a device allocation for the duration of one call, freed on every way out of it
+template <class X> struct DevTmp {
+  X* p = nullptr;
+  explicit DevTmp(size_t n) { LAPS_CK(cudaMalloc(&p, n * sizeof(X))); }
+  ~DevTmp() { if (p) cudaFree(p); }
+  DevTmp(const DevTmp&) = delete;
+  DevTmp& operator=(const DevTmp&) = delete;
+};
+
 class EngineBase {
  public:
   virtual ~EngineBase() {}
@@ -757,17 +766,13 @@ template <class T, class TS = T> class Engine : public EngineBase {
       LAPS_CK(cudaMemsetAsync(B.U, 0, 7 * g.fsc * sizeof(CS), stream));
       const int cnt = (int)hidx.size();
       if (cnt > 0) {
-        long long* didx = nullptr;
-        double2* dval = nullptr;
-        LAPS_CK(cudaMalloc(&didx, hidx.size() * sizeof(long long)));
-        LAPS_CK(cudaMalloc(&dval, hval.size() * sizeof(double2)));
-        LAPS_CK(cudaMemcpyAsync(didx, hidx.data(), hidx.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
-        LAPS_CK(cudaMemcpyAsync(dval, hval.data(), hval.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
-        k_place_modes<TS><<<(cnt + 255) / 256, 256, 0, stream>>>(B.U, g.fsc, didx, dval, cnt);
+        DevTmp<long long> didx(hidx.size());
+        DevTmp<double2> dval(hval.size());
+        LAPS_CK(cudaMemcpyAsync(didx.p, hidx.data(), hidx.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
+        LAPS_CK(cudaMemcpyAsync(dval.p, hval.data(), hval.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
+        k_place_modes<TS><<<(cnt + 255) / 256, 256, 0, stream>>>(B.U, g.fsc, didx.p, dval.p, cnt);
         LAPS_CK(cudaGetLastError());
         wait(tmo());
-        LAPS_CK(cudaFree(didx));
-        LAPS_CK(cudaFree(dval));
       }
       inverse3d(B.U, 7);  // the mode sums on the grid: W1 real fields 0..6
     }
@@ -869,42 +874,29 @@ template <class T, class TS = T> class Engine : public EngineBase {
     const int nl = naxis / 2;
     std::memset(hout, 0, 4 * (size_t)naxis * sizeof(double));
     if (nl < 1) return;
-    double* dmean = nullptr;
-    double* dout = nullptr;
-    double* part = nullptr;
     const int nblk = (int)std::min<long long>(4 * 152, (g.fsr + ANG_THREADS - 1) / ANG_THREADS);
-    LAPS_CK(cudaMalloc(&dmean, 4 * sizeof(double)));
-    LAPS_CK(cudaMalloc(&dout, 4 * (size_t)naxis * sizeof(double)));
-    LAPS_CK(cudaMalloc(&part, (size_t)nl * nblk * ANG_NSUM * sizeof(double)));
-    try {
-      k_state_means<TS><<<1, 32, 0, stream>>>(B.U, g.fsc, dmean);
-      LAPS_CK(cudaGetLastError());
-      double m[4];
-      LAPS_CK(cudaMemcpyAsync(m, dmean, sizeof(m), cudaMemcpyDeviceToHost, stream));
-      wait(tmo());
-      // statistics.c:86-101: b0 = <B> / |<B>|
-      const double b0abs = std::sqrt(m[1] * m[1] + m[2] * m[2] + m[3] * m[3]);
-      AngArgs a;
-      a.u = rs + 8 * g.fsr;
-      a.B = rs + 4 * g.fsr;
-      a.n = g.fsr;
-      a.nx = p.nx; a.ny = p.ny; a.nz = p.nz; a.axis = axis; a.lag0 = 1;
-      a.sqrt_rho0 = std::sqrt(m[0]);
-      a.b0x = m[1] / b0abs; a.b0y = m[2] / b0abs; a.b0z = m[3] / b0abs;
-      LAPS_CK(cudaMemsetAsync(dout, 0, 4 * (size_t)naxis * sizeof(double), stream));
-      k_angle_partial<<<dim3(nblk, nl), ANG_THREADS, 0, stream>>>(a, part);
-      LAPS_CK(cudaGetLastError());
-      k_angle_final<<<(nl + 127) / 128, 128, 0, stream>>>(part, nblk, nl, 1, naxis, dout);
-      LAPS_CK(cudaGetLastError());
-      LAPS_CK(cudaMemcpyAsync(hout, dout, 4 * (size_t)naxis * sizeof(double), cudaMemcpyDeviceToHost, stream));
-      wait(tmo());
-    } catch (...) {
-      cudaFree(dmean); cudaFree(dout); cudaFree(part);
-      throw;
-    }
-    LAPS_CK(cudaFree(dmean));
-    LAPS_CK(cudaFree(dout));
-    LAPS_CK(cudaFree(part));
+    DevTmp<double> dmean(4), dout(4 * (size_t)naxis), part((size_t)nl * nblk * ANG_NSUM);
+    k_state_means<TS><<<1, 32, 0, stream>>>(B.U, g.fsc, dmean.p);
+    LAPS_CK(cudaGetLastError());
+    double m[4];
+    LAPS_CK(cudaMemcpyAsync(m, dmean.p, sizeof(m), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
+    // statistics.c:86-101: b0 = <B> / |<B>|
+    const double b0abs = std::sqrt(m[1] * m[1] + m[2] * m[2] + m[3] * m[3]);
+    AngArgs a;
+    a.u = rs + 8 * g.fsr;
+    a.B = rs + 4 * g.fsr;
+    a.n = g.fsr;
+    a.nx = p.nx; a.ny = p.ny; a.nz = p.nz; a.axis = axis; a.lag0 = 1;
+    a.sqrt_rho0 = std::sqrt(m[0]);
+    a.b0x = m[1] / b0abs; a.b0y = m[2] / b0abs; a.b0z = m[3] / b0abs;
+    LAPS_CK(cudaMemsetAsync(dout.p, 0, 4 * (size_t)naxis * sizeof(double), stream));
+    k_angle_partial<<<dim3(nblk, nl), ANG_THREADS, 0, stream>>>(a, part.p);
+    LAPS_CK(cudaGetLastError());
+    k_angle_final<<<(nl + 127) / 128, 128, 0, stream>>>(part.p, nblk, nl, 1, naxis, dout.p);
+    LAPS_CK(cudaGetLastError());
+    LAPS_CK(cudaMemcpyAsync(hout, dout.p, 4 * (size_t)naxis * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    wait(tmo());
   }
   const laps_params& params() const override { return p; }
   long long grid_points() const override { return gfull.fsr; }
