@@ -6,16 +6,19 @@ Ur0/R0 = 0.01, eta = nu = 5e-4, 2/3 mask, cfl 0.4, random-phase 1 <= |k| <= 8 sp
 rms 0.5, seed 1), seeded synthetic initial condition.  A "step" is one full time step
 (CFL, three RK stages, radius update) of the whole grid.
 
-Our arm (default --precision fp32): the FP32-transform engine (FP32 transforms and nonlinear
-products; state, RK accumulation, CFL and diagnostics in float-float) through the C-ABI,
-timed beside the plain paths on the same workload (`plain`: the float-float engine, which
-matches FP64 to 1e-10, and the native FP64 engine) and with its error against the FP64
-engine stated (`error_vs_fp64`: per-field relative L2, invariants and the E(k) shell spectra
-after --err-steps steps).  `value` is device-timed with CUDA events on the engine's stream,
-state resident in HBM; `e2e` is the same metric through the C-ABI with host buffers (pinned
-upload of the primitive initial state, one laps_step call per step returning time/dt/status
-to the host, download of the final state).  --precision dd / fp64 / fp32_f64 time those
-modes as the headline instead.
+Our arm (default --precision fp32_f64): FP32 transforms and nonlinear products with the
+state, RK accumulation, CFL reduction and diagnostics in IEEE FP64 - the FP32-FFT option the
+target names - through the C-ABI, with its error against the FP64 engine stated over the
+workload's 500 steps (`error_vs_fp64`: per-field relative L2, invariants, time and the E(k)
+shell spectra of every shell up to k_max/2).  The other modes run beside it on the same
+workload (`plain`: "fp32" with a float-float state, "dd" the float-float engine that matches
+FP64 to 1e-10, "fp64" native binary64), each with its own roofline and end-to-end figure; the
+FP64 line also carries `fp64_roofline` (its transform flops against the FP64 pipe).
+`value` is device-timed with CUDA events on the engine's stream, state resident in HBM;
+`e2e` is the same metric through the C-ABI with host buffers (pinned upload of the primitive
+initial state, one laps_step call per step returning time/dt/status to the host, download of
+the final state).  `cufft_yardstick` times cuFFT's unfused transforms of the same fields
+beside the hand-written passes (outside the timed region).
 
 --impl reference: the reference's CPU algorithm (the oracle restatement, pocketfft with all
 host threads) timed on a bounded sample of the same workload.
@@ -195,7 +198,7 @@ def pass_bytes_3di(n, kx_keep, nky, nkz, eS=16, eT=16):
 
 def cpu_sample(steps, warmup, n=None):
     """The oracle restatement of the reference's step on the host cores: warmup + timed steps
-    at the full grid.  Returns (grid-point-steps/s, threads, sample text)."""
+    at the full grid.  Returns (grid-point-steps/s, threads, sample text, kind)."""
     from oracle import laps3d
 
     n = n or N_GRID
@@ -206,7 +209,8 @@ def cpu_sample(steps, warmup, n=None):
     for _ in range(steps):
         o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
     el = time.perf_counter() - t0
-    return n**3 * steps / el, laps3d._WORKERS, f"{warmup} warm-up + {steps} timed steps at {n}^3 (numpy + scipy.fft pocketfft)"
+    return (n**3 * steps / el, laps3d._WORKERS,
+            f"{warmup} warm-up + {steps} timed steps at {n}^3 (numpy + scipy.fft pocketfft)", "port")
 
 
 def fp32_error(p, prim, steps):
@@ -236,13 +240,12 @@ def fp32_error(p, prim, steps):
     out = {"steps": steps, "field_rel_l2": rel, "max_field_rel_l2": max(rel),
            "invariants_rel": [float(v) for v in np.abs(a[1] - b[1]) / np.maximum(np.abs(b[1]), 1e-300)],
            "time_rel": abs(a[2] - b[2]) / b[2],
-           "spectrum_shells": f"1..{half.stop - 1}"}
+           "spectrum_shells": f"1..{half.stop - 1} (every shell up to k_max/2, k_max = n/3)"}
     for key, i in (("u", 3), ("b", 4)):
         ea, eb = a[i][half], b[i][half]
         relk = np.abs(ea - eb) / np.maximum(eb, 1e-300)
-        live = eb >= 1e-6 * eb.max()  # shells holding at least 1e-6 of the largest
         out[f"spectrum_{key}_rel_by_shell"] = [float(f"{v:.3g}") for v in relk]
-        out[f"spectrum_{key}_max_rel_live_shells"] = float(relk[live].max())
+        out[f"spectrum_{key}_max_rel"] = float(relk.max())
         out[f"spectrum_{key}_max_abs_over_total"] = float(np.abs(ea - eb).max() / eb.sum())
     return out
 
@@ -260,6 +263,199 @@ def device_timed(p, prim, steps, warmup):
     pass_ms, total_ms, status = g.step_profiled(steps)
     g.close()
     return pass_ms, total_ms, status, info
+
+
+def pinned_buffers(prim, local):
+    """Page-locked host arrays (torch's pinned allocator) for the end-to-end leg, so the
+    copies run at link speed; plain numpy arrays when torch cannot pin."""
+    try:
+        import torch
+
+        torch.cuda.set_device(local)
+
+        def pinned_array(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+        host_in = pinned_array(prim.shape)
+        host_in[...] = prim
+        return host_in, pinned_array((8,) + prim.shape[1:]), pinned_array((4,) + prim.shape[1:]), True
+    except Exception:
+        return (np.ascontiguousarray(prim), np.empty((8,) + prim.shape[1:]), np.empty((4,) + prim.shape[1:]), False)
+
+
+def end_to_end(p, bufs, steps, npts, ws):
+    """The metric through the C-ABI with host buffers: upload of the primitive state from
+    pinned host memory, `steps` laps_step(1) calls (each returns time, dt and status to the
+    host), download of the final conserved state and primitives; host clock, max over ranks.
+    One untimed pass of the same sequence warms the path first."""
+    import ctypes
+
+    from laps_gb300 import ffi
+
+    lib = ffi.load()
+    host_in, host_out, host_prim, pinned = bufs
+    dptr = ctypes.POINTER(ctypes.c_double)
+    ctx = ffi.Laps(p)
+    ctx.upload_state(host_in, primitive=True)
+    ctx.set_time(0.0)
+    ctx.step(2)
+    assert lib.laps_download_state(ctx.h, host_out.ctypes.data_as(dptr), host_prim.ctypes.data_as(dptr)) == 0
+    barrier(ws)
+    t0 = time.perf_counter()
+    ctx.upload_state(host_in, primitive=True)
+    ctx.set_time(0.0)
+    t1 = time.perf_counter()
+    for _ in range(steps):
+        ctx.step(1)
+    t2 = time.perf_counter()
+    assert lib.laps_download_state(ctx.h, host_out.ctypes.data_as(dptr), host_prim.ctypes.data_as(dptr)) == 0
+    t3 = time.perf_counter()
+    ctx.close()
+    e2e_s = barrier_max(t3 - t0, ws)
+    return {"value": ws * npts * steps / e2e_s, "unit": "grid-point-steps/s",
+            "h2d_bytes_per_step": host_in.nbytes / steps + 16,
+            "d2h_bytes_per_step": (host_out.nbytes + host_prim.nbytes) / steps + 128,
+            "pinned": pinned, "upload_s": t1 - t0, "steps_s": t2 - t1, "download_s": t3 - t2}
+
+
+def roofline_of(pass_ms, steps, info, mode, n, workload):
+    """Dominant pass of a mode: its algorithmic bytes (pass_bytes) over its average
+    event-timed launch against the measured copy bandwidth, and the same figure for every
+    pass; `traffic` is the ncu DRAM bytes of one launch of that pass (profiles/traffic.json,
+    captured on a reduced grid and scaled by the planes processed), when present."""
+    eS, eT = PRECISIONS[mode][2:4]
+    pbf = pass_bytes_3di if WL["variant"] == 1 else pass_bytes
+    pb = pbf(n, info.kx_keep, info.ky_keep, info.kz_keep, eS=eS, eT=eT) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
+    launches = steps * 3
+    dom = max(range(5), key=lambda i: pass_ms[i])
+    name = PASS_NAMES[dom]
+    avg_ms = pass_ms[dom] / launches
+    achieved = pb[name] / (avg_ms * 1e-3) / 1e9 if pb[name] else None
+    peak, src = peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists() and not SHAPE and n == WL["grid"]:
+        try:
+            traffic = json.loads(tf.read_text()).get(f"{workload}/{mode}", {}).get(name)
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "peak_source": src, "traffic": traffic,
+            "algorithmic_bytes_per_launch": pb[name]}
+    per_pass = {PASS_NAMES[i]: {"gbs": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9,
+                                "frac": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9 / peak}
+                for i in range(5) if pb[PASS_NAMES[i]] and pass_ms[i] > 0}
+    return roof, per_pass
+
+
+# FP64 issue rate of this GPU's FP64 pipe: FMA/ADD instructions per second, measured with
+# independent dependency chains on a GB300 (~1.6 per clock per SM at 2.07 GHz).  A flop rate
+# counts an FMA as two.
+FP64_INSTR_PER_S = 0.508e12
+
+
+def fp64_roofline(pass_ms, steps, n, info):
+    """The plain FP64 path against the FP64 pipe: the transform flops of pass C (24 real
+    transforms of the x rows: 11 inverse, 13 forward, 2.5 n log2 n each, the benchFFT count)
+    over its average launch, against 2 x the measured FP64 FMA issue rate."""
+    c_ms = pass_ms[2] / (steps * 3)
+    rows = n * n
+    flops = 24 * rows * 2.5 * n * math.log2(n)
+    achieved = flops / (c_ms * 1e-3) / 1e12
+    peak = 2 * FP64_INSTR_PER_S / 1e12
+    return {"bound": "fp64", "kernel": "C_x_flux", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "flops_per_launch": flops,
+            "flop_count": "transforms only (2.5 n log2 n per real line); the flux physics adds more"}
+
+
+def cufft_yardstick(n, pass_ms, steps, kind):
+    """cuFFT (through torch.fft) on the same 256^3 fields: the transforms each pass does,
+    unfused and unpruned, as batched R2C/C2R along x and C2C along y and z, in the pass's
+    transform precision.  Outside the timed `value`; a yardstick for the hand-written
+    passes, whose times include the physics, the RK update and the pruning."""
+    import torch
+
+    cdt = torch.complex64 if kind == "f32" else torch.complex128
+    rdt = torch.float32 if kind == "f32" else torch.float64
+    nh = n // 2 + 1
+    dev = "cuda"
+    # (pass, what cuFFT does): fields per launch of the compressible Hall + expanding-box stage
+    jobs = {
+        "A_inv_z": ("c2c_z", 10), "B_inv_y": ("c2c_y", 11), "C_x_flux": ("c2r_r2c_x", (11, 13)),
+        "D_fwd_y": ("c2c_y", 13), "E_fwd_z_rk": ("c2c_z", 13),
+    }
+    out = {}
+    spec = torch.randn((13, n, n, nh), dtype=cdt, device=dev)
+    real = torch.randn((13, n, n, n), dtype=rdt, device=dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(reps):
+            fn()
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    for name, (op, nf) in jobs.items():
+        if op == "c2c_z":
+            ms = timed(lambda: torch.fft.ifft(spec[:nf], dim=1))
+        elif op == "c2c_y":
+            ms = timed(lambda: torch.fft.fft(spec[:nf], dim=2))
+        else:
+            ms = timed(lambda: torch.fft.irfft(spec[:nf[0]], n=n, dim=3)) + timed(lambda: torch.fft.rfft(real[:nf[1]], dim=3))
+        ours = pass_ms[PASS_NAMES.index(name)] / (steps * 3)
+        out[name] = {"cufft_ms": ms, "ours_ms": ours, "ours_over_cufft": ours / ms}
+    del spec, real
+    torch.cuda.empty_cache()
+    tot_c = sum(v["cufft_ms"] for v in out.values())
+    tot_o = sum(v["ours_ms"] for v in out.values())
+    return {"library": f"cuFFT via torch.fft (torch {torch.__version__})", "precision": kind, "per_stage": out,
+            "stage_cufft_ms": tot_c, "stage_ours_ms": tot_o, "ours_over_cufft": tot_o / tot_c,
+            "note": "cuFFT: transforms only, all modes; ours: the fused passes with physics, RK update and dealias "
+                    "pruning"}
+
+
+def measure_mode(mode, p0, prim, args, npts, bufs, ws, local, with_clocks=False):
+    """One arithmetic mode on the workload: device-timed steps (CUDA events around every pass,
+    state resident in HBM), the graph path, the end-to-end leg, and the roofline figures."""
+    from laps_gb300 import ffi
+
+    q = ffi.laps_params.from_buffer_copy(p0)
+    q.precision = PRECISIONS[mode][0]
+    g = ffi.Laps(q)
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    g.step(max(args.warmup, 3))
+    info = g.info()
+    barrier(ws)
+    clk = Clocks(local) if with_clocks else None
+    if clk:
+        clk.__enter__()
+    pass_ms, total_ms, status = g.step_profiled(args.steps)
+    if clk:
+        clk.__exit__()
+    barrier(ws)
+    tmax = barrier_max(total_ms, ws)
+    t0 = time.perf_counter()
+    g.step(args.steps)  # the graph path (what laps_step replays), same state continuing
+    graph_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    g.close()
+    n = N_GRID
+    roof, per_pass = roofline_of(pass_ms, args.steps, info, mode, n, args.workload)
+    res = {"value": ws * npts * args.steps / (tmax * 1e-3), "ms_per_step": tmax / args.steps, "status": status,
+           "dtype": PRECISIONS[mode][1], "graph_ms_per_step": graph_ms,
+           "pass_ms_per_step": {PASS_NAMES[i]: pass_ms[i] / args.steps for i in range(6)},
+           "roofline": roof, "passes_hbm": per_pass,
+           "e2e": end_to_end(q, bufs, args.steps, npts, ws),
+           "_info": info, "_pass_ms": pass_ms}
+    if clk:
+        res["clocks"] = clk.summary()
+    if mode == "fp64" and not SHAPE and WL["variant"] == 0:
+        res["fp64_roofline"] = fp64_roofline(pass_ms, args.steps, n, info)
+    return res
 
 
 def run_ensemble(args):
@@ -325,14 +521,14 @@ def run_reference(args):
         return 0
     k = max(1, min(args.steps, args.ref_steps))
     w = min(args.warmup, 1)
-    v, cores, sample = cpu_sample(k, w)
+    v, cores, sample, kind = cpu_sample(k, w)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-point-steps/s", "n_gpus": args.gpus,
         "steps": k, "warmup": w, "ms_per_step": N_GRID**3 / v * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-phase spectrum)",
         "config": {"workload": WORKLOAD, "grid": N_GRID, "variant": "3DC", "hall": 0.05, "expanding_box": "Ur0/R0=0.01",
                    "dealias": "2/3 sphere", "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -347,139 +543,55 @@ def run_ours(args):
         dist.init_process_group("gloo")
     from laps_gb300 import ffi
 
-    prec = PRECISIONS[args.precision][0]
     n = N_GRID
     prim = initial_state()
     nx, ny, nz = SHAPE if SHAPE else (n, n, n)
     npts = nx * ny * nz
-    p = ffi.params(nx=nx, ny=ny, nz=nz, precision=prec, device=local, variant=WL["variant"], **WL["kw"])
-    g = ffi.Laps(p)
-    g.upload_state(prim, primitive=True)
-    g.set_time(0.0)
-    g.step(max(args.warmup, 3) if args.warmup >= 3 else args.warmup)
-    info = g.info()
-    # ---- device-resident timed region: K steps, CUDA events around every pass
-    barrier(ws)
-    with Clocks(local) as clk:
-        pass_ms, total_ms, status = g.step_profiled(args.steps)
-    barrier(ws)
-    tmax = barrier_max(total_ms, ws)
-    value = ws * npts * args.steps / (tmax * 1e-3)
-    # ---- graph path, same state continues (reported beside)
-    t0 = time.perf_counter()
-    g.step(args.steps)
-    graph_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    # ---- end to end through the C-ABI with host buffers
-    import ctypes
-
-    lib = ffi.load()
-    try:  # page-locked host buffers (torch's pinned allocator) so the copies run at link speed
-        import torch
-
-        torch.cuda.set_device(local)
-
-        def pinned_array(shape):
-            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-
-        host_in = pinned_array(prim.shape)
-        host_in[...] = prim
-        host_out = pinned_array((8,) + prim.shape[1:])
-        host_prim = pinned_array((4,) + prim.shape[1:])
-        pinned = True
-    except Exception:
-        host_in = np.ascontiguousarray(prim)
-        host_out = np.empty((8,) + prim.shape[1:])
-        host_prim = np.empty((4,) + prim.shape[1:])
-        pinned = False
-    e2e_ctx = ffi.Laps(p)
-    e2e_ctx.upload_state(host_in, primitive=True)  # warm the path once: upload, steps, download
-    e2e_ctx.set_time(0.0)
-    e2e_ctx.step(2)
-    rc = lib.laps_download_state(e2e_ctx.h, host_out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                 host_prim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
-    assert rc == 0
-    barrier(ws)
-    t0 = time.perf_counter()
-    e2e_ctx.upload_state(host_in, primitive=True)
-    e2e_ctx.set_time(0.0)
-    t1 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_ctx.step(1)  # returns time, dt, status to the host every step
-    t2 = time.perf_counter()
-    rc = lib.laps_download_state(e2e_ctx.h, host_out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                 host_prim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
-    assert rc == 0
-    t3 = time.perf_counter()
-    e2e_s = barrier_max(t3 - t0, ws)
-    e2e_parts = {"upload_s": t1 - t0, "steps_s": t2 - t1, "download_s": t3 - t2}
-    e2e_v = ws * npts * args.steps / e2e_s
-    h2d = host_in.nbytes / args.steps + 16
-    d2h = (host_out.nbytes + host_prim.nbytes) / args.steps + 128
-    e2e_ctx.close()
-    g.close()
-    # ---- the plain paths on the same workload (FP64-parity float-float, native FP64)
+    p = ffi.params(nx=nx, ny=ny, nz=nz, precision=PRECISIONS[args.precision][0], device=local,
+                   variant=WL["variant"], **WL["kw"])
+    bufs = pinned_buffers(prim, local)
+    head = measure_mode(args.precision, p, prim, args, npts, bufs, ws, local, with_clocks=True)
+    info = head.pop("_info")
+    pass_ms = head.pop("_pass_ms")
+    # ---- the other arithmetic modes on the same workload (rank 0 of a single run)
     plain = {}
     if not args.no_plain and rank == 0 and ws == 1:
-        for mode in ("dd", "fp64"):
+        for mode in ("fp32", "dd", "fp64"):
             if mode == args.precision:
                 continue
-            q = ffi.laps_params.from_buffer_copy(p)
-            q.precision = PRECISIONS[mode][0]
-            pm, tm, st_p, _ = device_timed(q, prim, args.steps, max(args.warmup, 3))
-            v = npts * args.steps / (tm * 1e-3)
-            plain[mode] = {"value": v, "ms_per_step": tm / args.steps, "status": st_p,
-                           "dtype": PRECISIONS[mode][1],
-                           "pass_ms_per_step": {PASS_NAMES[i]: pm[i] / args.steps for i in range(6)}}
-    # ---- roofline of the dominant pass
-    nky, nkz = info.ky_keep, info.kz_keep
-    eS, eT = PRECISIONS[args.precision][2:4]
-    pbf = pass_bytes_3di if WL["variant"] == 1 else pass_bytes
-    pb = pbf(n, info.kx_keep, nky, nkz, eS=eS, eT=eT) if not SHAPE else {k: 0 for k in PASS_NAMES[:5]}
-    launches = args.steps * 3
-    dom = max(range(5), key=lambda i: pass_ms[i])
-    name = PASS_NAMES[dom]
-    avg_ms = pass_ms[dom] / launches
-    achieved = pb[name] / (avg_ms * 1e-3) / 1e9 if pb[name] else None
-    peak, src = peaks()
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            key = f"{args.workload}/{args.precision}"
-            if not SHAPE and n == WL["grid"]:
-                traffic = json.loads(tf.read_text()).get(key, {}).get(name)
-        except Exception:
-            traffic = None
+            r = measure_mode(mode, p, prim, args, npts, bufs, ws, local)
+            r.pop("_info"), r.pop("_pass_ms")
+            plain[mode] = r
     line = {
-        "metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": head["value"], "unit": "grid-point-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": PRECISIONS[args.precision][1],
         "data": WL["data"],
         "config": dict({"workload": WORKLOAD, "grid": n, "precision": args.precision}, **WL["desc"],
                        parallelism=f"replicas x{ws}", l2=f"inputs larger than L2 ({info.device_bytes / 1e9:.0f} GB working set)"),
         "gpu_launches": args.steps * info.kernels_per_step,
-        "status": status,
-        "graph_ms_per_step": graph_ms,
-        "pass_ms_per_step": {PASS_NAMES[i]: pass_ms[i] / args.steps for i in range(6)},
-        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "peak_source": src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": pb[name]},
-        # every FFT pass: algorithmic bytes over its event-timed launch, against the same peak
-        "passes_hbm": {PASS_NAMES[i]: {"gbs": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9,
-                                       "frac": pb[PASS_NAMES[i]] / (pass_ms[i] / launches * 1e-3) / 1e9 / peak}
-                       for i in range(5) if pb[PASS_NAMES[i]] and pass_ms[i] > 0},
-        "e2e": {"value": e2e_v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "pinned": pinned, **e2e_parts},
-        "clocks": clk.summary(),
+        "status": head["status"],
+        "graph_ms_per_step": head["graph_ms_per_step"],
+        "pass_ms_per_step": head["pass_ms_per_step"],
+        "roofline": head["roofline"],
+        "passes_hbm": head["passes_hbm"],
+        "e2e": head["e2e"],
+        "clocks": head["clocks"],
     }
     if plain:
         line["plain"] = plain
-        line["vs_plain"] = {k: value / v["value"] for k, v in plain.items()}
-    if args.precision.startswith("fp32") and not SHAPE and not args.no_err:
+        line["vs_plain"] = {k: head["value"] / v["value"] for k, v in plain.items()}
+    if rank == 0 and ws == 1 and not SHAPE and not args.no_cufft and WL["variant"] == 0:
+        try:
+            line["cufft_yardstick"] = cufft_yardstick(n, pass_ms, args.steps,
+                                                      "f32" if args.precision.startswith("fp32") else "f64")
+        except Exception as e:  # torch without CUDA, or out of memory: say so
+            line["cufft_yardstick"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    if args.precision.startswith("fp32") and not SHAPE and not args.no_err and rank == 0:
         line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
     if rank == 0 and ws == 1 and not args.no_cpu and WL["variant"] == 0:
-        v, cores, sample = cpu_sample(1, 0)
-        line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample, kind = cpu_sample(args.cpu_steps, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": kind, "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -496,15 +608,20 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=list(PRECISIONS))
+    ap.add_argument("--precision", default="fp32_f64", choices=list(PRECISIONS),
+                    help="headline mode: fp32_f64 (FP32 transforms and products, FP64 state / RK / CFL / "
+                         "diagnostics: the FP32-FFT option), fp32 (the same with a float-float state), dd, fp64")
     ap.add_argument("--workload", default="c3d256", choices=["c3d256", "c3di512", "ens2d"],
                     help="c3d256: the 3-D Hall + expanding-box case (headline); c3di512: the 3-D incompressible "
                          "FP32-vs-FP64 study at 512^3; ens2d: the 2-D ensemble")
     ap.add_argument("--members", type=int, default=64, help="ensemble members (--workload ens2d)")
     ap.add_argument("--no-plain", action="store_true", dest="no_plain",
                     help="skip timing the plain float-float and FP64 paths beside the headline mode")
-    ap.add_argument("--err-steps", type=int, default=10, dest="err_steps",
-                    help="steps of the FP32-vs-FP64 error check of the fp32 modes")
+    ap.add_argument("--err-steps", type=int, default=500, dest="err_steps",
+                    help="steps of the FP32-vs-FP64 error check of the fp32 modes (the workload's step count)")
+    ap.add_argument("--no-cufft", action="store_true", dest="no_cufft", help="skip the cuFFT yardstick")
+    ap.add_argument("--cpu-steps", type=int, default=1, dest="cpu_steps",
+                    help="timed steps of the CPU baseline (after one warm-up step)")
     ap.add_argument("--no-err", action="store_true", dest="no_err")
     ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
     ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")

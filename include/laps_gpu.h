@@ -295,19 +295,20 @@ const char* laps_batch_last_error(laps_batch* b); /* NULL: the last laps_batch_c
 
 /* Forward transform of nfields real FP64 fields that allocates no device memory, for hosts
  * that cannot call cudaMalloc (their device memory comes from their own pool or framework,
- * or allocation is not allowed after start-up).  No counterpart in the reference: it is the
- * transform of laps_upload_state (transform_uu_real_to_fourier, fftw.f90:42-71) run on
- * buffers the caller owns.
+ * or allocation is not allowed after start-up).  It has no counterpart in the reference: it
+ * runs the same forward transform as laps_upload_state on buffers the caller owns.
  *   uu: device pointer, uu(nx,ny,nz,nfields) float64;  uf: device pointer,
  *   uu_fourier(nx/2+1,ny,nz,nfields) interleaved complex float64;  stream: a cudaStream_t
  *   (NULL: the default stream).  The call is asynchronous on that stream.
  * The intermediate half spectrum of one field lives in a fixed 32 MiB device array inside
  * the library, which every GPU that loads the library holds until the process exits; grids
  * whose padded half spectrum ((nx/2+1 rounded up to 8) * ny * nz) exceeds 2^21 complex
- * elements - 128^3 fits - are rejected with LAPS_EINVAL.  The first call on a device looks
- * up the array's address with that device current; make that first call before any stream
- * capture.  Every call shares the array, so calls that overlap on the GPU (other streams,
- * other host threads) race.  Errors are reported through laps_last_error(NULL). */
+ * elements - 128^3 fits - are rejected with LAPS_EINVAL.  Every call looks up the array's
+ * device address with the caller's device and context current (so a cudaDeviceReset between
+ * calls is safe); the first call in a context also loads the library's kernels there, so make
+ * that first call before any stream capture.  Every call shares the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race.  Errors are reported through
+ * laps_last_error(NULL). */
 int laps_transform_uu_real_to_fourier_noalloc(const double* uu, double* uf, int nx, int ny, int nz, int nfields,
                                               void* stream);
 

@@ -78,11 +78,15 @@ inline CUtensorMap work_tensor_map(void* base, const Geo& g, int nfields, int ew
   return m;
 }
 
-// a device allocation for the duration of one call, freed on every way out of it
+// a device allocation for the duration of one call, freed on every way out of it.  Both
+// the allocation and the free are ordered on the call's stream (cudaMallocAsync /
+// cudaFreeAsync), so a call that gives up on a bounded wait returns at once: the free waits
+// on the device for the kernels still using the buffer instead of blocking the host.
 template <class X> struct DevTmp {
   X* p = nullptr;
-  explicit DevTmp(size_t n) { LAPS_CK(cudaMalloc(&p, n * sizeof(X))); }
-  ~DevTmp() { if (p) cudaFree(p); }
+  cudaStream_t s;
+  DevTmp(size_t n, cudaStream_t stream) : s(stream) { LAPS_CK(cudaMallocAsync((void**)&p, n * sizeof(X), s)); }
+  ~DevTmp() { if (p) cudaFreeAsync(p, s); }
   DevTmp(const DevTmp&) = delete;
   DevTmp& operator=(const DevTmp&) = delete;
 };
@@ -766,8 +770,8 @@ template <class T, class TS = T> class Engine : public EngineBase {
       LAPS_CK(cudaMemsetAsync(B.U, 0, 7 * g.fsc * sizeof(CS), stream));
       const int cnt = (int)hidx.size();
       if (cnt > 0) {
-        DevTmp<long long> didx(hidx.size());
-        DevTmp<double2> dval(hval.size());
+        DevTmp<long long> didx(hidx.size(), stream);
+        DevTmp<double2> dval(hval.size(), stream);
         LAPS_CK(cudaMemcpyAsync(didx.p, hidx.data(), hidx.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
         LAPS_CK(cudaMemcpyAsync(dval.p, hval.data(), hval.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
         k_place_modes<TS><<<(cnt + 255) / 256, 256, 0, stream>>>(B.U, g.fsc, didx.p, dval.p, cnt);
@@ -875,7 +879,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     std::memset(hout, 0, 4 * (size_t)naxis * sizeof(double));
     if (nl < 1) return;
     const int nblk = (int)std::min<long long>(4 * 152, (g.fsr + ANG_THREADS - 1) / ANG_THREADS);
-    DevTmp<double> dmean(4), dout(4 * (size_t)naxis), part((size_t)nl * nblk * ANG_NSUM);
+    DevTmp<double> dmean(4, stream), dout(4 * (size_t)naxis, stream), part((size_t)nl * nblk * ANG_NSUM, stream);
     k_state_means<TS><<<1, 32, 0, stream>>>(B.U, g.fsc, dmean.p);
     LAPS_CK(cudaGetLastError());
     double m[4];

@@ -14,15 +14,9 @@ namespace laps {
 
 // complex elements of the scratch half spectrum: room for one field of a 128^3 grid
 constexpr long long NOALLOC_MAX_ELEMS = 1LL << 21;  // 32 MiB of double2
-constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) double2 g_noalloc_scratch[NOALLOC_MAX_ELEMS];
 static __device__ __align__(256) double2 g_noalloc_tw[3 * 512];  // x, y, z tables at 0, 512, 1024
-
-// device addresses of the two arrays, looked up once per device
-static double2* g_scratch_ptr[NOALLOC_MAX_DEVICES];
-static double2* g_tw_ptr[NOALLOC_MAX_DEVICES];
-static bool g_ready[NOALLOC_MAX_DEVICES];
 
 // exp(-2 pi i j / n) for the three axes
 __global__ void k_noalloc_twiddles(double2* tw, int nx, int ny, int nz) {
@@ -72,19 +66,15 @@ extern "C" int laps_transform_uu_real_to_fourier_noalloc(const double* uu, doubl
   }
   cudaStream_t s = (cudaStream_t)stream;
   try {
-    int dev = 0;
-    LAPS_CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) throw Error{LAPS_EINVAL, "device ordinal out of range"};
-    if (!g_ready[dev]) {  // set-up, once per device, with that device current
-      void* p = nullptr;
-      LAPS_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-      g_scratch_ptr[dev] = (double2*)p;
-      LAPS_CK(cudaGetSymbolAddress(&p, g_noalloc_tw));
-      g_tw_ptr[dev] = (double2*)p;
-      g_ready[dev] = true;
-    }
-    double2* scr = g_scratch_ptr[dev];
-    double2* tw = g_tw_ptr[dev];
+    // The arrays' device addresses are looked up on every call, with the caller's device and
+    // context current: a cached address would go stale when the host resets the device
+    // (cudaDeviceReset reloads the module at new addresses) or switches contexts, and the
+    // lookup allocates nothing.  The first lookup in a context loads the module there.
+    void* p = nullptr;
+    LAPS_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    double2* scr = (double2*)p;
+    LAPS_CK(cudaGetSymbolAddress(&p, g_noalloc_tw));
+    double2* tw = (double2*)p;
     k_noalloc_twiddles<<<2, 256, 0, s>>>(tw, nx, ny, nz);
     LAPS_CK(cudaGetLastError());
     const long long rows = (long long)ny * nz;

@@ -13,7 +13,8 @@ import os
 import subprocess
 from pathlib import Path
 
-REF = Path(os.environ.get("LAPS_REFERENCE_DIR", "/root/reference"))
+# the reference tree: LAPS_REFERENCE_DIR, else a checkout named "reference" beside this repository
+REF = Path(os.environ.get("LAPS_REFERENCE_DIR") or Path(__file__).resolve().parents[2] / "reference")
 OUT = Path(__file__).resolve().parent / "_ref"
 LIB = OUT / "libangle_ref.so"
 
