@@ -20,8 +20,10 @@ initial state, one laps_step call per step returning time/dt/status to the host,
 the final state).  `cufft_yardstick` times cuFFT's unfused transforms of the same fields
 beside the hand-written passes (outside the timed region).
 
---impl reference: the reference's CPU algorithm (the oracle restatement, pocketfft with all
-host threads) timed on a bounded sample of the same workload.
+--impl reference: the reference's CPU algorithm on the machine's host cores - the C++/OpenMP
+restatement with its own FFT (oracle/laps3d_omp.cpp; the reference itself needs Fortran, MPI
+and FFTW, which the box does not have) - timed over the same --warmup / --steps of the same
+workload; `cpu_baseline` in our arm is the same code on a 1 + 3 step sample.
 
 For N > 1 (torchrun) every rank advances its own independent replica ("replicas only":
 one run does not shard); value = all ranks' grid-point-steps / the slowest rank's time.
@@ -197,12 +199,30 @@ def pass_bytes_3di(n, kx_keep, nky, nkz, eS=16, eT=16):
 
 
 def cpu_sample(steps, warmup, n=None):
-    """The oracle restatement of the reference's step on the host cores: warmup + timed steps
-    at the full grid.  Returns (grid-point-steps/s, threads, sample text, kind)."""
+    """The reference's step restated for the host cores: the C++/OpenMP restatement
+    (oracle/laps3d_omp.cpp, its own FFT, FP64, every host thread) - warmup + timed steps of
+    the full grid.  Falls back to the numpy restatement where g++ / OpenMP cannot build it.
+    Returns (grid-point-steps/s, threads, sample text, kind)."""
+    n = n or N_GRID
+    prim = initial_state(n)
+    try:
+        from oracle import laps3d_omp
+
+        r = laps3d_omp.Run(n, CFG2)
+        r.set_state(prim)
+        if warmup:
+            r.step(warmup)
+        t0 = time.perf_counter()
+        r.step(steps)
+        el = time.perf_counter() - t0
+        r.close()
+        return (n**3 * steps / el, laps3d_omp.threads(),
+                f"{warmup} warm-up + {steps} timed steps at {n}^3 (C++/OpenMP restatement, own radix-2 FFT, FP64)", "port")
+    except (OSError, ValueError, subprocess.CalledProcessError):
+        pass
     from oracle import laps3d
 
-    n = n or N_GRID
-    o = laps3d.restart(n, CFG2, initial_state(n))
+    o = laps3d.restart(n, CFG2, prim)
     for _ in range(warmup):
         o.vardt(); o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
     t0 = time.perf_counter()
@@ -519,8 +539,8 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    k = max(1, min(args.steps, args.ref_steps))
-    w = min(args.warmup, 1)
+    k = max(1, args.steps if args.ref_steps <= 0 else min(args.steps, args.ref_steps))
+    w = args.warmup
     v, cores, sample, kind = cpu_sample(k, w)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-point-steps/s", "n_gpus": args.gpus,
@@ -620,10 +640,11 @@ def main():
     ap.add_argument("--err-steps", type=int, default=500, dest="err_steps",
                     help="steps of the FP32-vs-FP64 error check of the fp32 modes (the workload's step count)")
     ap.add_argument("--no-cufft", action="store_true", dest="no_cufft", help="skip the cuFFT yardstick")
-    ap.add_argument("--cpu-steps", type=int, default=1, dest="cpu_steps",
+    ap.add_argument("--cpu-steps", type=int, default=3, dest="cpu_steps",
                     help="timed steps of the CPU baseline (after one warm-up step)")
     ap.add_argument("--no-err", action="store_true", dest="no_err")
-    ap.add_argument("--ref-steps", type=int, default=2, dest="ref_steps")
+    ap.add_argument("--ref-steps", type=int, default=0, dest="ref_steps",
+                    help="cap on the timed steps of --impl reference (0: the same --steps as our arm)")
     ap.add_argument("--no-cpu", action="store_true", dest="no_cpu")
     ap.add_argument("--grid", type=int, default=256, help="grid size n (n^3); the headline workload is 256")
     ap.add_argument("--shape", default=None, help="nx,ny,nz of a reduced profiling case (overrides --grid)")

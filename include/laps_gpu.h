@@ -312,6 +312,35 @@ const char* laps_batch_last_error(laps_batch* b); /* NULL: the last laps_batch_c
 int laps_transform_uu_real_to_fourier_noalloc(const double* uu, double* uf, int nx, int ny, int nz, int nfields,
                                               void* stream);
 
+/* ---------------------------------------------------------------- learned subgrid closure
+ * 3x3x3 periodic convolutions in BF16 on the tensor cores (FP32 accumulation), the layers of
+ * the subgrid-stress net that closes a coarse incompressible run.  No counterpart in the
+ * reference: the closure is an addition, and the plain solver above is its fallback.
+ * All pointers are device pointers; calls are asynchronous on `stream` (a cudaStream_t, NULL:
+ * the default stream) and allocate nothing.  Errors: laps_last_error(NULL).
+ *
+ * Activation layout: channels-last BF16 with a one-voxel periodic halo on x: element
+ * (z, y, xp, c) at ((z*ny + y)*(nx + 2) + xp)*C + c with xp = x + 1, xp = 0 and nx + 1 holding
+ * the values at x = nx - 1 and x = 0; C, the padded channel count, is 16 or 32 (channels past
+ * the layer's own count are zero).  nx is a multiple of 128; buffers are 16-byte aligned.
+ *
+ * laps_conv3_pack: weights w[cout][cin][3][3][3] (float32, the cross-correlation
+ *   out[x] = sum_k w[k] in[x + k - 1], k = 0..2 per axis) into the tensor cores' operand
+ *   layout, 27 * cin_p * cout_p BF16 values at wpk.  flip = 1 packs the input-gradient layer
+ *   instead (channels exchanged, taps mirrored): its forward with act 2 is the backward pass
+ *   of the layer with respect to its input.
+ * laps_conv3_forward: y = act(conv(x) + bias) over the whole periodic grid, x with cin_p
+ *   channels, y (halo written) with cout_p.  act 0: linear; act 1: GELU (exact, erf form),
+ *   the pre-activation written to zpre when zpre is not NULL; act 2: y = conv(x) * GELU'(gate),
+ *   gate a pre-activation with cout_p channels (the backward pass through the previous layer's
+ *   activation), bias unused.
+ * laps_conv3_status: wait for the stream, then read and clear the convolutions' error word
+ *   (*err = 1 when a bounded wait inside a convolution ran out; its output is then invalid). */
+int laps_conv3_pack(const float* w, void* wpk, int cin, int cout, int cin_p, int cout_p, int flip, void* stream);
+int laps_conv3_forward(const void* x, const void* wpk, const float* bias, void* y, void* zpre, const void* gate,
+                       int nx, int ny, int nz, int cin_p, int cout_p, int act, void* stream);
+int laps_conv3_status(void* stream, int* err);
+
 /* Bounded wait for all queued work of the context. */
 int laps_wait(laps_ctx* ctx, int timeout_ms);
 

@@ -49,19 +49,6 @@ template <class T> std::vector<typename Store<T>::C> twiddles(int n) {
   return t;
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
-inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    LAPS_CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !p) throw Error{LAPS_ECUDA, "cuTensorMapEncodeTiled is not available"};
-    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
-
 // A work buffer of nfields fields seen by the tile copies: 8-byte elements, dim 0 = kx
 // (kxp * ew elements, ew = complex bytes / 8), dim 1 = y, dim 2 = z + field * nz; box
 // {TX * ew, by, bz}.

@@ -3,6 +3,7 @@
 // so that the float-float FFT code compiles in parallel.
 #pragma once
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <string>
 #include "passes.cuh"
 
@@ -31,6 +32,19 @@ inline int mass_rk_blocks(const Geo& g) {
   const long long tot = (long long)g.kx_keep * g.nky() * g.nkz();
   const long long nb = (tot + 255) / 256;
   return (int)(nb < 4 * 152 ? (nb > 0 ? nb : 1) : 4 * 152);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    LAPS_CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw Error{LAPS_ECUDA, "cuTensorMapEncodeTiled is not available"};
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
 }
 
 template <class K> inline void set_smem(K kernel, int bytes) {
