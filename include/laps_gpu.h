@@ -334,11 +334,17 @@ int laps_transform_uu_real_to_fourier_noalloc(const double* uu, double* uf, int 
  *   the pre-activation written to zpre when zpre is not NULL; act 2: y = conv(x) * GELU'(gate),
  *   gate a pre-activation with cout_p channels (the backward pass through the previous layer's
  *   activation), bias unused.
+ * laps_conv3_wgrad: the weight gradient of a layer, dw[t][co][ci] = sum over the grid of
+ *   dz(v, co) * x(v + shift(t), ci) (float32, 27 x cout_p x cin_p, tap t = (kz*3 + ky)*3 + kx,
+ *   overwritten), x the layer's input (cin_p channels), dz the gradient at its pre-activation
+ *   output (cout_p channels, halo not read); nx a multiple of 64.
  * laps_conv3_status: wait for the stream, then read and clear the convolutions' error word
  *   (*err = 1 when a bounded wait inside a convolution ran out; its output is then invalid). */
 int laps_conv3_pack(const float* w, void* wpk, int cin, int cout, int cin_p, int cout_p, int flip, void* stream);
 int laps_conv3_forward(const void* x, const void* wpk, const float* bias, void* y, void* zpre, const void* gate,
                        int nx, int ny, int nz, int cin_p, int cout_p, int act, void* stream);
+int laps_conv3_wgrad(const void* x, const void* dz, float* dw, int nx, int ny, int nz, int cin_p, int cout_p,
+                     void* stream);
 int laps_conv3_status(void* stream, int* err);
 
 /* Bounded wait for all queued work of the context. */
