@@ -233,31 +233,57 @@ def cpu_sample(steps, warmup, n=None):
             f"{warmup} warm-up + {steps} timed steps at {n}^3 (numpy + scipy.fft pocketfft)", "port")
 
 
-def fp32_error(p, prim, steps):
-    """Error of an FP32-transform run against the FP64 engine after `steps` steps of the same
-    workload (the FP64 engine matches the oracle to 1e-10): per-field relative L2, the
-    invariants, the time, and the shell spectra E_u(k), E_b(k) over 1 <= k <= k_max / 2
-    (k_max = n/3, the 2/3 sphere)."""
+def fp32_error(p, prim, steps, chunk=25):
+    """Error of an FP32-transform run against the FP64 engine (which matches the oracle to
+    1e-10) on the same workload: per-field relative L2, the invariants, the time and the shell
+    spectra E_u(k), E_b(k) of every shell 1 <= k <= k_max / 2 (k_max = n/3, the 2/3 sphere).
+    Both runs advance in chunks of `chunk` steps.  If the FP64 run collapses first - the CFL
+    step below 1 % of its first value, or the dt floor - the statement is the last checkpoint
+    before the collapse, and `collapse` records where it happened."""
     from laps_gb300 import ffi
 
     nshell = max(p.nx, p.ny, p.nz) // 3 + 1
-    runs = {}
+    ctx = {}
     for name, mode in (("test", p.precision), ("fp64", ffi.PREC_FP64)):
         q = ffi.laps_params.from_buffer_copy(p)
         q.precision = mode
         r = ffi.Laps(q)
         r.upload_state(prim, primitive=True)
         r.set_time(0.0)
-        t, dt, st = r.step(steps)
-        uu, _ = r.download_state()
-        d = r.diagnostics()
-        eu, eb = r.spectrum(nshell)
-        runs[name] = (uu, np.array([d.e_kin, d.e_mag, d.h_cross, d.h_mag]), t, eu, eb)
+        ctx[name] = r
+
+    def snapshot():
+        out = {}
+        for name, r in ctx.items():
+            uu, _ = r.download_state()
+            d = r.diagnostics()
+            eu, eb = r.spectrum(nshell)
+            t, dt = r.time()
+            out[name] = (uu, np.array([d.e_kin, d.e_mag, d.h_cross, d.h_mag]), t, eu, eb, dt)
+        return out
+
+    done, dt0, good, collapse = 0, None, None, None
+    while done < steps:
+        k = min(chunk, steps - done)
+        st = {name: r.step(k)[2] for name, r in ctx.items()}
+        done += k
+        t64, dt64 = ctx["fp64"].time()
+        dt0 = dt0 or dt64
+        if st["fp64"] != 0 or dt64 < 0.01 * dt0:
+            collapse = {"step_checkpoint": done, "time": t64, "dt": dt64, "status": st["fp64"],
+                        "note": "the FP64 run (the reference's algorithm) collapsed: CFL step below 1 % of its "
+                                "first value or the dt floor; the statement is the last checkpoint before it"}
+            break
+        good = (done, snapshot())
+    for r in ctx.values():
         r.close()
-    a, b = runs["test"], runs["fp64"]
+    if good is None:
+        return {"steps": 0, "collapse": collapse}
+    nsteps, snap = good
+    a, b = snap["test"], snap["fp64"]
     rel = [float(np.linalg.norm(a[0][f] - b[0][f]) / max(np.linalg.norm(b[0][f]), 1e-300)) for f in range(8)]
     half = slice(1, (nshell - 1) // 2 + 1)
-    out = {"steps": steps, "field_rel_l2": rel, "max_field_rel_l2": max(rel),
+    out = {"steps": nsteps, "steps_requested": steps, "time": b[2], "field_rel_l2": rel, "max_field_rel_l2": max(rel),
            "invariants_rel": [float(v) for v in np.abs(a[1] - b[1]) / np.maximum(np.abs(b[1]), 1e-300)],
            "time_rel": abs(a[2] - b[2]) / b[2],
            "spectrum_shells": f"1..{half.stop - 1} (every shell up to k_max/2, k_max = n/3)"}
@@ -267,6 +293,8 @@ def fp32_error(p, prim, steps):
         out[f"spectrum_{key}_rel_by_shell"] = [float(f"{v:.3g}") for v in relk]
         out[f"spectrum_{key}_max_rel"] = float(relk.max())
         out[f"spectrum_{key}_max_abs_over_total"] = float(np.abs(ea - eb).max() / eb.sum())
+    if collapse:
+        out["collapse"] = collapse
     return out
 
 
@@ -609,6 +637,18 @@ def run_ours(args):
             line["cufft_yardstick"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     if args.precision.startswith("fp32") and not SHAPE and not args.no_err and rank == 0:
         line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
+        if WL["variant"] == 0:
+            # The workload's recipe (rms 0.5 on a beta 0.2 background) is far from pressure
+            # balance: its magnetic-pressure fluctuations drive the pressure negative and the
+            # FP64 run collapses to the dt floor near t = 0.28 (step ~250 at 256^3) under the
+            # reference's own algorithm.  The full step count is stated on the same recipe at
+            # rms 0.1, which stays pressure-positive.
+            from laps_gb300.ic import turbulence_ic
+
+            low = turbulence_ic(N_GRID, kmin=1, kmax=8, alpha=-1.0, rms_u=0.1, rms_b=0.1, seed=1)
+            e = fp32_error(p, low, args.err_steps)
+            e["workload"] = "the same recipe at rms 0.1 (pressure stays positive for the whole run)"
+            line["error_vs_fp64_rms01"] = e
     if rank == 0 and ws == 1 and not args.no_cpu and WL["variant"] == 0:
         v, cores, sample, kind = cpu_sample(args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": kind, "sample": sample}

@@ -330,7 +330,8 @@ int laps_transform_uu_real_to_fourier_noalloc(const double* uu, double* uf, int 
  *   instead (channels exchanged, taps mirrored): its forward with act 2 is the backward pass
  *   of the layer with respect to its input.
  * laps_conv3_forward: y = act(conv(x) + bias) over the whole periodic grid, x with cin_p
- *   channels, y (halo written) with cout_p.  act 0: linear; act 1: GELU (exact, erf form),
+ *   channels, y (halo written) with cout_p; bias holds cout_p floats, zero past the layer's own
+ *   channels (or is NULL).  act 0: linear; act 1: GELU (exact, erf form),
  *   the pre-activation written to zpre when zpre is not NULL; act 2: y = conv(x) * GELU'(gate),
  *   gate a pre-activation with cout_p channels (the backward pass through the previous layer's
  *   activation), bias unused.

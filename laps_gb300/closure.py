@@ -86,7 +86,10 @@ def conv3(x, wpk, cout_p: int, bias=None, act: int = 0, zpre=None, gate=None, ou
     nz, ny, nxp, cin_p = x.shape
     nx = nxp - 2
     y = out if out is not None else torch.empty((nz, ny, nxp, cout_p), dtype=torch.bfloat16, device=x.device)
-    b = bias.float().contiguous() if bias is not None else None
+    b = None
+    if bias is not None:  # the kernels read cout_p entries: zeros past the layer's channels
+        b = torch.zeros(cout_p, dtype=torch.float32, device=x.device)
+        b[: bias.numel()] = bias.float()
     _ck(_lib().laps_conv3_forward(x.data_ptr(), wpk.data_ptr(), b.data_ptr() if b is not None else None, y.data_ptr(),
                                   zpre.data_ptr() if zpre is not None else None,
                                   gate.data_ptr() if gate is not None else None, nx, ny, nz, cin_p, cout_p, act,

@@ -241,4 +241,80 @@ template <> struct Cvt<double, float> {
 };
 template <class D, class S> __device__ __forceinline__ cx<D> cvtc(cx<S> v) { return {Cvt<D, S>::r(v.re), Cvt<D, S>::r(v.im)}; }
 
+// ------------------------------------------------------- FP32 <-> FP64 on the integer pipes
+// Conversions written on the IEEE 754 bit fields with integer instructions, for kernels whose
+// FP64 pipe is the bottleneck (on GB300 a conversion to or from binary64 issues at the FP64
+// pipe's rate, ~1/70 of FP32).  f32_to_f64_bits is exact for normal numbers, zeros,
+// infinities and NaN (a subnormal float becomes a signed zero).  f64_to_f32_trunc rounds the
+// significand toward zero (within one FP32 ulp of the value), flushes magnitudes below the
+// FP32 normal range to a signed zero, maps larger ones to infinity and keeps NaN a NaN.
+__host__ __device__ __forceinline__ uint64_t f64_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  __builtin_memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double f64_from_bits(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  __builtin_memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  __builtin_memcpy(&b, &x, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ float f32_from_bits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  __builtin_memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ double f32_to_f64_bits(float x) {
+  const uint32_t b = f32_bits(x);
+  const uint32_t sign = b & 0x80000000u, e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  const uint32_t de = e == 0xffu ? 0x7ffu : e + 896u;  // rebias 127 -> 1023
+  const uint32_t hi = e == 0 ? sign : (sign | (de << 20) | (m >> 3));
+  const uint32_t lo = e == 0 ? 0u : (m << 29);
+  return f64_from_bits(((uint64_t)hi << 32) | lo);
+}
+__host__ __device__ __forceinline__ float f64_to_f32_trunc(double x) {
+  const uint64_t d = f64_bits(x);
+  const uint32_t hi = (uint32_t)(d >> 32), lo = (uint32_t)d;
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu), fe = e - 896;  // rebias 1023 -> 127
+  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  uint32_t b;
+  if (e == 0x7ff) b = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
+  else if (fe <= 0) b = sign;
+  else if (fe >= 255) b = sign | 0x7f800000u;
+  else b = sign | ((uint32_t)fe << 23) | m;
+  return f32_from_bits(b);
+}
+
+// An FP32 view of a state-type value and a state-type value of an FP32 increment, as the
+// FP32-increment RK update needs them (binary64: through the bit fields above).
+template <class T> struct IncCvt {
+  __device__ __forceinline__ static cx<float> to_f32(cx<T> v) { return cvtc<float>(v); }
+  __device__ __forceinline__ static cx<T> from_f32(cx<float> v) { return cvtc<T>(v); }
+};
+template <> struct IncCvt<double> {
+  __device__ __forceinline__ static cx<float> to_f32(cx<double> v) { return {f64_to_f32_trunc(v.re), f64_to_f32_trunc(v.im)}; }
+  __device__ __forceinline__ static cx<double> from_f32(cx<float> v) { return {f32_to_f64_bits(v.re), f32_to_f64_bits(v.im)}; }
+};
+
 }  // namespace laps

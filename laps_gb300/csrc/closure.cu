@@ -47,7 +47,7 @@ constexpr int CONV_THREADS = 192;  // producer warp, MMA warp, 4 epilogue warps
 struct ConvArgs {
   int nx, ny, nz, ntiles;
   int act;                      // 0 linear, 1 GELU (keeps the pre-activation), 2 gradient gate
-  const float* bias;            // [N] or null
+  const float* bias;            // [N] (zero past the layer's own channels) or null
   const __nv_bfloat16* gate;    // act 2: pre-activation z of the layer whose output is the input
   __nv_bfloat16* y;             // output, padded layout, N channels
   __nv_bfloat16* zpre;          // act 1: pre-activation (padded layout) or null

@@ -998,7 +998,7 @@ struct RkCtx {
                                              int kx, int ky, int kz, const PT<float>& cf, float ccf, float ddcf,
                                              float itf, float tsf) const {
     const bool mom = v >= 1 && v <= 3, mag = v >= 4 && v <= 6;
-    const cx<float> uf = cvtc<float>(u);
+    const cx<float> uf = IncCvt<T>::to_f32(u);
     if (P->aeb && (P->ebm_mask >> v & 1)) fnl = fnl - uf * (cf.ebm[v] * itf);
     if (mom && P->visc && P->visc_exp) fnl = fnl - uf * (cf.nu * k2f);
     if (mag && P->resis && P->resis_exp && !(P->cons_bg && kx == 0 && kz == 0)) fnl = fnl - uf * (cf.eta * k2f);
@@ -1019,7 +1019,7 @@ struct RkCtx {
     if ((P->dealias == 1 || P->dealias == 3) && kx >= K->kxlim[kz * g->ny + ky]) {
       un = cx_zero<T>();
     } else {
-      un = u + cvtc<T>(inc);
+      un = u + IncCvt<T>::from_f32(inc);
       if (P->dealias == 2) un = ((un * K->fx[kx]) * K->fy[ky]) * K->fz[kz];
     }
     Store<T>::stc(U, un);
@@ -1143,16 +1143,20 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
   // elements in chunks of CH: the state and RK-register loads of a chunk are issued together
   // ahead of its arithmetic (the update's stores may alias them as far as the compiler knows)
   constexpr int CH = CL::EPT < 4 ? CL::EPT : 4;
+  // the RK register as the update reads it: FP32 as stored for FP32 increments, else in TS
+  using RV = typename std::conditional<F32INC, float, TS>::type;
 #pragma unroll 1
   for (int m0 = 0; m0 < CL::EPT; m0 += CH) {
-    cx<TS> uo[CH], ro[CH];
+    cx<TS> uo[CH];
+    cx<RV> ro[CH];
 #pragma unroll
     for (int i = 0; i < CH; i++) {
       const int kz = x.j(m0 + i);
       const long long idx = kz * zs;
       const bool in = g.kz_in(kz);
       uo[i] = in ? Store<TS>::ldc(U + idx) : cx_zero<TS>();
-      ro[i] = in ? rk.r_of(R + idx) : cx_zero<TS>();
+      if constexpr (F32INC) ro[i] = in && a.stage > 0 ? Store<T>::ldc(R + idx) : cx_zero<float>();
+      else ro[i] = in ? rk.r_of(R + idx) : cx_zero<TS>();
     }
 #pragma unroll
     for (int i = 0; i < CH; i++) {
@@ -1169,7 +1173,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
       }
       if constexpr (F32INC) {
         const float k2f = need_k2 ? Cvt<float, T>::r(rkf.k2(kx, ky, kz)) : 0.0f;
-        rk.update_f32(v, f, uo[i], cvtc<float>(ro[i]), U + idx, R + idx, k2f, kx, ky, kz, pc, ccf, ddcf, itf, tsf);
+        rk.update_f32(v, f, uo[i], ro[i], U + idx, R + idx, k2f, kx, ky, kz, pc, ccf, ddcf, itf, tsf);
       } else {
         TS k2 = need_k2 ? rk.k2(kx, ky, kz) : kk.ps.zero;
         rk.update(v, cvtc<TS>(f), uo[i], ro[i], U + idx, R + idx, k2, kx, ky, kz);
