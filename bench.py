@@ -466,6 +466,61 @@ def cufft_yardstick(n, pass_ms, steps, kind):
                     "pruning"}
 
 
+def bf16_peak():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def closure_conv_bench(n=128, reps=20):
+    """The closure net's tensor-core convolutions on the coarse grid (n^3, periodic): one
+    32 -> 32 channel 3x3x3 layer forward with GELU, its input-gradient and its weight-gradient
+    kernels, timed with CUDA events on the stream they run on; TFLOP/s = 2 x voxels x 27 x 32 x
+    32 per kernel over its average time, against the dense BF16 peak."""
+    import torch
+
+    from laps_gb300 import closure
+
+    dev = "cuda"
+    g = torch.Generator(device=dev).manual_seed(4)
+    x = torch.randn((n, n, n + 2, 32), device=dev, generator=g).to(torch.bfloat16)
+    dz = torch.randn((n, n, n + 2, 32), device=dev, generator=g).to(torch.bfloat16)
+    w = torch.randn((32, 32, 3, 3, 3), device=dev, generator=g) * 0.05
+    b = torch.zeros(32, device=dev)
+    pk, pkf = closure.pack(w, 32, 32), closure.pack(w, 32, 32, flip=True)
+    y = torch.empty_like(x)
+    zp = torch.empty_like(x)
+    runs = {
+        "forward_gelu": lambda: closure.conv3(x, pk, 32, bias=b, act=1, zpre=zp, out=y),
+        "input_gradient": lambda: closure.conv3(dz, pkf, 32, act=2, gate=zp, out=y),
+        "weight_gradient": lambda: closure.wgrad(x, dz, 32, 32),
+    }
+    flops = 2.0 * n**3 * 27 * 32 * 32
+    peak, src = bf16_peak()
+    out = {"grid": f"{n}^3", "channels": "32 -> 32", "flops_per_kernel": flops, "peak_tflops": peak,
+           "peak_source": src}
+    s = torch.cuda.current_stream()
+    for name, fn in runs.items():
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        tf = flops / (ms * 1e-3) / 1e12
+        out[name] = {"ms": ms, "tflops": tf, "frac": tf / peak}
+    out["status"] = closure.status()
+    # algorithmic bytes of the forward layer: input read once, output and pre-activation written
+    fwd_bytes = 3 * n * n * (n + 2) * 32 * 2
+    out["forward_gelu"]["hbm_gbs"] = fwd_bytes / (out["forward_gelu"]["ms"] * 1e-3) / 1e9
+    return out
+
+
 def measure_mode(mode, p0, prim, args, npts, bufs, ws, local, with_clocks=False):
     """One arithmetic mode on the workload: device-timed steps (CUDA events around every pass,
     state resident in HBM), the graph path, the end-to-end leg, and the roofline figures."""
@@ -635,6 +690,11 @@ def run_ours(args):
                                                       "f32" if args.precision.startswith("fp32") else "f64")
         except Exception as e:  # torch without CUDA, or out of memory: say so
             line["cufft_yardstick"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    if rank == 0 and ws == 1 and not SHAPE and not args.no_closure:
+        try:
+            line["closure_conv"] = closure_conv_bench()
+        except Exception as e:
+            line["closure_conv"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     if args.precision.startswith("fp32") and not SHAPE and not args.no_err and rank == 0:
         line["error_vs_fp64"] = fp32_error(p, prim, args.err_steps)
         if WL["variant"] == 0:
@@ -680,6 +740,8 @@ def main():
     ap.add_argument("--err-steps", type=int, default=500, dest="err_steps",
                     help="steps of the FP32-vs-FP64 error check of the fp32 modes (the workload's step count)")
     ap.add_argument("--no-cufft", action="store_true", dest="no_cufft", help="skip the cuFFT yardstick")
+    ap.add_argument("--no-closure", action="store_true", dest="no_closure",
+                    help="skip the closure convolutions' tensor-core measurement")
     ap.add_argument("--cpu-steps", type=int, default=3, dest="cpu_steps",
                     help="timed steps of the CPU baseline (after one warm-up step)")
     ap.add_argument("--no-err", action="store_true", dest="no_err")

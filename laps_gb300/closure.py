@@ -115,3 +115,68 @@ def status() -> int:
     e = C.c_int(0)
     _ck(_lib().laps_conv3_status(_stream(), C.byref(e)))
     return e.value
+
+
+# ------------------------------------------------------------------------------ the net
+LAYERS = ((6, 32, 1), (32, 32, 1), (32, 32, 1), (32, 12, 0))  # (in, out, GELU) per layer
+
+
+class ClosureNet:
+    """The subgrid-stress net: 4 periodic 3x3x3 convolutions (6 -> 32 -> 32 -> 32 -> 12,
+    GELU between them) run by the tcgen05 kernels in BF16 with FP32 accumulation.  Master
+    weights and biases are FP32 torch tensors; `forward` keeps what `backward` needs (the
+    layer inputs and pre-activations, in the kernels' padded layout) and `backward` returns
+    the FP32 gradients of every weight and bias for the gradient at the output."""
+
+    def __init__(self, device="cuda", seed=0, layers=LAYERS):
+        import torch
+
+        g = torch.Generator().manual_seed(seed)
+        self.layers = layers
+        self.w, self.b = [], []
+        for cin, cout, _ in layers:
+            w = torch.randn((cout, cin, 3, 3, 3), generator=g) * (2.0 / (27 * cin)) ** 0.5
+            self.w.append(w.to(device).requires_grad_(True))
+            self.b.append(torch.zeros(cout, device=device).requires_grad_(True))
+        self.device = device
+        self.repack()
+
+    def parameters(self):
+        return self.w + self.b
+
+    def repack(self):
+        """BF16 operands of the current master weights (forward and input-gradient forms)."""
+        self.pk, self.pkf = [], []
+        for (cin, cout, _), w in zip(self.layers, self.w):
+            ci, co = padded_channels(cin), padded_channels(cout)
+            self.pk.append(pack(w, ci, co))
+            self.pkf.append(pack(w, ci, co, flip=True))
+
+    def forward(self, x):
+        """x: (nz, ny, nx + 2, 16) padded BF16 input.  Returns the padded output (16 channels,
+        12 used)."""
+        import torch
+
+        self.acts, self.pre = [x], []
+        a = x
+        for l, (cin, cout, act) in enumerate(self.layers):
+            co = padded_channels(cout)
+            z = torch.empty(a.shape[:3] + (co,), dtype=torch.bfloat16, device=a.device) if act else None
+            a = conv3(a, self.pk[l], co, bias=self.b[l].detach(), act=act, zpre=z)
+            self.pre.append(z)
+            self.acts.append(a)
+        return a
+
+    def backward(self, dy):
+        """dy: gradient at the output, padded layout (halo filled).  Sets .grad of every
+        weight and bias (FP32)."""
+        g = dy
+        for l in range(len(self.layers) - 1, -1, -1):
+            cin, cout, _ = self.layers[l]
+            nx = g.shape[2] - 2
+            self.w[l].grad = wgrad(self.acts[l], g, cin, cout).contiguous()
+            self.b[l].grad = g[:, :, 1:nx + 1, :cout].float().sum(dim=(0, 1, 2))
+            if l > 0:  # through this layer's input and the previous activation's GELU
+                ci = padded_channels(cin)
+                g = conv3(g, self.pkf[l], ci, act=2, gate=self.pre[l - 1])
+        return g

@@ -245,9 +245,10 @@ template <class D, class S> __device__ __forceinline__ cx<D> cvtc(cx<S> v) { ret
 // Conversions written on the IEEE 754 bit fields with integer instructions, for kernels whose
 // FP64 pipe is the bottleneck (on GB300 a conversion to or from binary64 issues at the FP64
 // pipe's rate, ~1/70 of FP32).  f32_to_f64_bits is exact for normal numbers, zeros,
-// infinities and NaN (a subnormal float becomes a signed zero).  f64_to_f32_trunc rounds the
-// significand toward zero (within one FP32 ulp of the value), flushes magnitudes below the
-// FP32 normal range to a signed zero, maps larger ones to infinity and keeps NaN a NaN.
+// infinities and NaN (a subnormal float becomes a signed zero).  f64_to_f32_rn rounds to the
+// nearest float, ties to even (the carry of the rounding increment runs into the exponent and
+// on to infinity), flushes magnitudes below the FP32 normal range to a signed zero, maps
+// larger ones to infinity and keeps NaN a NaN.
 __host__ __device__ __forceinline__ uint64_t f64_bits(double x) {
 #ifdef __CUDA_ARCH__
   return (uint64_t)__double_as_longlong(x);
@@ -292,17 +293,18 @@ __host__ __device__ __forceinline__ double f32_to_f64_bits(float x) {
   const uint32_t lo = e == 0 ? 0u : (m << 29);
   return f64_from_bits(((uint64_t)hi << 32) | lo);
 }
-__host__ __device__ __forceinline__ float f64_to_f32_trunc(double x) {
+__host__ __device__ __forceinline__ float f64_to_f32_rn(double x) {
   const uint64_t d = f64_bits(x);
   const uint32_t hi = (uint32_t)(d >> 32), lo = (uint32_t)d;
   const uint32_t sign = hi & 0x80000000u;
   const int e = (int)((hi >> 20) & 0x7ffu), fe = e - 896;  // rebias 1023 -> 127
-  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // the 23 kept significand bits
+  const uint32_t rem = lo & 0x1fffffffu;                    // the 29 dropped ones
   uint32_t b;
   if (e == 0x7ff) b = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
   else if (fe <= 0) b = sign;
   else if (fe >= 255) b = sign | 0x7f800000u;
-  else b = sign | ((uint32_t)fe << 23) | m;
+  else b = (sign | ((uint32_t)fe << 23) | m) + ((rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u);
   return f32_from_bits(b);
 }
 
@@ -313,7 +315,7 @@ template <class T> struct IncCvt {
   __device__ __forceinline__ static cx<T> from_f32(cx<float> v) { return cvtc<T>(v); }
 };
 template <> struct IncCvt<double> {
-  __device__ __forceinline__ static cx<float> to_f32(cx<double> v) { return {f64_to_f32_trunc(v.re), f64_to_f32_trunc(v.im)}; }
+  __device__ __forceinline__ static cx<float> to_f32(cx<double> v) { return {f64_to_f32_rn(v.re), f64_to_f32_rn(v.im)}; }
   __device__ __forceinline__ static cx<double> from_f32(cx<float> v) { return {f32_to_f64_bits(v.re), f32_to_f64_bits(v.im)}; }
 };
 

@@ -143,6 +143,11 @@ template <class T, class TS = T> class Engine : public EngineBase {
   Bufs<T, TS> B{};
   C *twx = nullptr, *twy = nullptr, *twz = nullptr;      // twiddles in T (passes)
   CS *twxs = nullptr, *twys = nullptr, *twzs = nullptr;  // twiddles in TS (state transforms)
+  // FP32 transforms with an FP64 state: the per-field state transforms of upload and download
+  // run in float-float on the FP32 pipes (48-bit significand; native FP64 transforms are
+  // FP64-pipe bound, ~7x slower here), with the values converted at both ends
+  static constexpr bool XDD = std::is_same<T, float>::value && std::is_same<TS, double>::value;
+  float4 *twxd = nullptr, *twyd = nullptr, *twzd = nullptr;  // float-float twiddles (XDD)
   SRS *s_wx, *s_kxd, *s_wy, *s_kyd, *s_kzd, *s_kx2, *s_ky2, *s_kz2, *s_fx = nullptr, *s_fy = nullptr, *s_fz = nullptr;
   SR *t_wx, *t_kxd, *t_wy, *t_kyd, *t_kzd, *t_kx2, *t_ky2, *t_kz2, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr;
   double *d_wx, *d_wy, *d_wz;
@@ -316,6 +321,12 @@ template <class T, class TS = T> class Engine : public EngineBase {
     twxs = dalloc<CS>(q.nx); up(twxs, twxs_h);
     twys = dalloc<CS>(q.ny); up(twys, twys_h);
     twzs = dalloc<CS>(q.nz); up(twzs, twzs_h);
+    if constexpr (XDD) {
+      auto twxd_h = twiddles<dd>(q.nx), twyd_h = twiddles<dd>(q.ny), twzd_h = twiddles<dd>(q.nz);
+      twxd = dalloc<float4>(q.nx); up(twxd, twxd_h);
+      twyd = dalloc<float4>(q.ny); up(twyd, twyd_h);
+      twzd = dalloc<float4>(q.nz); up(twzd, twzd_h);
+    }
     d_wx = dalloc<double>(g.nh); up(d_wx, wx);
     d_wy = dalloc<double>(q.ny); up(d_wy, wy);
     d_wz = dalloc<double>(q.nz); up(d_wz, wz);
@@ -624,15 +635,39 @@ template <class T, class TS = T> class Engine : public EngineBase {
     LAPS_CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
     for (auto& e : fev) LAPS_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
-  // one real field -> its spectrum through the intermediate tmp (one spectral field)
+  // one real field -> its spectrum through the intermediate tmp (one spectral field); the
+  // float-float route (XDD) converts the real field in place, so its input is consumed
   void forward_one(const SRS* real, CS* out, CS* tmp) {
     const Geo& g = gfull;
+    if constexpr (XDD) {
+      float2* rd = (float2*)const_cast<SRS*>(real);
+      float4* td = (float4*)tmp;
+      k_f64_to_dd<<<1024, 256, 0, stream>>>((const double*)real, rd, g.fsr);
+      LAPS_CK(cudaGetLastError());
+      launch_rows_r2c<dd>(stream, p.nx, rd, td, (long long)g.ny * g.nz, g.kxp, twxd);
+      launch_col_plain<dd>(stream, td, td, g.fsc, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twyd);
+      launch_col_plain<dd>(stream, td, td, g.fsc, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twzd);
+      k_dd_to_f64<<<1024, 256, 0, stream>>>((const float2*)td, (double*)out, 2 * g.fsc);
+      LAPS_CK(cudaGetLastError());
+      return;
+    }
     rows_r2c(real, tmp, (long long)g.ny * g.nz);
     col_plain(tmp, tmp, 1, g.ny, -1, g.kxp, g.ny * g.kxp, g.nh, g.nz, -ilog2(g.ny), twys);
     col_plain(tmp, out, 1, g.nz, -1, g.ny * g.kxp, g.kxp, g.nh, g.ny, -ilog2(g.nz), twzs);
   }
   void inverse_one(const CS* spec, SRS* real, CS* tmp) {
     const Geo& g = gfull;
+    if constexpr (XDD) {
+      float4* td = (float4*)tmp;
+      k_f64_to_dd<<<1024, 256, 0, stream>>>((const double*)spec, (float2*)td, 2 * g.fsc);
+      LAPS_CK(cudaGetLastError());
+      launch_col_plain<dd>(stream, td, td, g.fsc, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twzd);
+      launch_col_plain<dd>(stream, td, td, g.fsc, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twyd);
+      launch_rows_c2r<dd>(stream, p.nx, td, (float2*)real, (long long)g.ny * g.nz, g.kxp, twxd);
+      k_dd_to_f64<<<1024, 256, 0, stream>>>((const float2*)real, (double*)real, g.fsr);
+      LAPS_CK(cudaGetLastError());
+      return;
+    }
     col_plain(spec, tmp, 1, g.nz, +1, g.ny * g.kxp, g.kxp, g.nh, g.ny, 0, twzs);
     col_plain(tmp, tmp, 1, g.ny, +1, g.kxp, g.ny * g.kxp, g.nh, g.nz, 0, twys);
     rows_c2r(tmp, real, (long long)g.ny * g.nz);

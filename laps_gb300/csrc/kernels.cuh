@@ -314,6 +314,25 @@ __global__ void k_upload_field(const double* __restrict__ h, typename Store<T>::
 }
 
 // real T field -> float64 (the conserved fields of the pipelined download)
+// FP64 <-> float-float, for the FP64-state transforms of the FP32-transform engine, which run
+// in float-float: the bit-field conversions of arith.cuh and one FP64 subtraction or addition
+// per value (a value keeps 48 significand bits).  n values; in place allowed (same bytes).
+static __global__ void k_f64_to_dd(const double* in, float2* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double x = in[i];
+    const float hi = f64_to_f32_rn(x);
+    const float lo = f64_to_f32_rn(x - f32_to_f64_bits(hi));
+    const dd v = dd_fast_two_sum(hi, lo);
+    out[i] = make_float2(v.hi, v.lo);
+  }
+}
+static __global__ void k_dd_to_f64(const float2* in, double* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = f32_to_f64_bits(v.x) + f32_to_f64_bits(v.y);
+  }
+}
+
 template <class T>
 __global__ void k_field_to_double(const typename Store<T>::R* __restrict__ u, double* __restrict__ h, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

@@ -105,7 +105,9 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
     int kz = x.j(m);
     cx<T> v = cx_zero<T>();
     if (ok && g.kz_in(kz)) {
-      v = cvtc<T>(Store<TS>::ldc(raw + kz * TX + x.c));
+      // (FP32 lines of an FP64 state: the conversion on the integer pipes)
+      if constexpr (std::is_same<T, float>::value) v = IncCvt<TS>::to_f32(Store<TS>::ldc(raw + kz * TX + x.c));
+      else v = cvtc<T>(Store<TS>::ldc(raw + kz * TX + x.c));
       if (e.mult < 0) v = -mul_i(v, K.kzd[kz]);
       else if (e.mult > 0) v = mul_i(v, K.kzd[kz]);
     }

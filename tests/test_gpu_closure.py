@@ -143,3 +143,61 @@ def test_rejects_bad_shapes():
     wpk = torch.zeros(27 * 32 * 32, dtype=torch.bfloat16, device=dev)
     with pytest.raises(ffi.LapsError):
         closure.conv3(x, wpk, 32)  # nx = 64 is not a multiple of 128
+
+
+def test_net_gradients_match_autograd():
+    """The whole 4-layer net (6 -> 32 -> 32 -> 32 -> 12, GELU) forward and backward through
+    the C-ABI kernels against torch autograd of the same net in float64 on BF16-rounded
+    inputs: outputs within 2^-6, every weight and bias gradient within 3e-2 of the
+    largest entry of its tensor (gradients pass through three BF16-rounded activations)."""
+    shape = (128, 8, 6)
+    nx, ny, nz = shape
+    dev = "cuda"
+    net = closure.ClosureNet(device=dev, seed=5)
+    g = torch.Generator().manual_seed(9)
+    x = _bf(torch.randn((6, nz, ny, nx), generator=g, dtype=torch.float64))
+    target = torch.randn((12, nz, ny, nx), generator=g, dtype=torch.float64) * 0.1
+    # reference: float64 autograd of the same net on the BF16-rounded weights
+    ws = [_bf(w.detach().double().cpu()).requires_grad_(True) for w in net.w]
+    bs = [b.detach().double().cpu().requires_grad_(True) for b in net.b]
+    a = x
+    for l, (cin, cout, act) in enumerate(closure.LAYERS):
+        z = _conv_ref(a, ws[l], bs[l])
+        a = _gelu(z) if act else z
+    loss = ((a - target) ** 2).sum() / 2
+    loss.backward()
+    y = net.forward(closure.to_padded(x.to(dev)))
+    yo = closure.from_padded(y, 12).double().cpu()
+    # four BF16 roundings of activations on the way: the output bound is 2^-6
+    ref = a.detach()
+    scale = ref.abs() + 1e-2 * ref.pow(2).mean().sqrt()
+    assert ((yo - ref).abs() / scale).max().item() <= 2.0 ** -6
+    dy = closure.to_padded((yo - target).to(dev))  # d loss / d y, BF16 padded with its halo
+    net.backward(dy)
+    assert closure.status() == 0
+    for l in range(4):
+        for got, ref in ((net.w[l].grad, ws[l].grad), (net.b[l].grad, bs[l].grad)):
+            err = ((got.double().cpu() - ref).abs().max() / ref.abs().max()).item()
+            assert err < 3e-2, (l, err)
+
+
+def test_training_reduces_the_loss():
+    """A few Adam steps on a fixed input/target pair through the tcgen05 kernels lower the loss."""
+    shape = (128, 8, 4)
+    nx, ny, nz = shape
+    dev = "cuda"
+    net = closure.ClosureNet(device=dev, seed=6)
+    g = torch.Generator().manual_seed(10)
+    x = closure.to_padded(torch.randn((6, nz, ny, nx), generator=g).to(dev))
+    t = torch.randn((12, nz, ny, nx), generator=g).to(dev) * 0.3
+    opt = torch.optim.Adam(net.parameters(), lr=3e-3)
+    losses = []
+    for _ in range(30):
+        y = net.forward(x)
+        r = closure.from_padded(y, 12) - t
+        losses.append(float((r ** 2).mean()))
+        net.backward(closure.to_padded(2 * r / r.numel()))
+        opt.step()
+        net.repack()
+    assert closure.status() == 0
+    assert losses[-1] < 0.7 * losses[0], losses
