@@ -266,6 +266,15 @@ int laps_dealias(laps_ctx* ctx);
 int laps_transform_uu_k2r(laps_ctx* ctx, double* uu);
 int laps_update_prim(laps_ctx* ctx, double* uu_prim);
 
+/* Device-side exchange for a caller that works on the GPU (the learned closure), no
+ * counterpart in the reference.  Both wait for the context's stream.
+ *   laps_state_real_device: the conserved real state uu(nx,ny,nz,1:8) (as laps_download_state
+ *     gives it) into uu_dev, a device buffer of 8*nx*ny*nz doubles.
+ *   laps_add_spectral_device: uu_fourier += scale * duf_dev for the 8 fields, duf_dev a device
+ *     array in the layout of laps_download_spectral, then the dealias mask or filter. */
+int laps_state_real_device(laps_ctx* ctx, double* uu_dev);
+int laps_add_spectral_device(laps_ctx* ctx, const double* duf_dev, double scale);
+
 /* The reference's output / restart file outNNN.dat (mhdoutput.f90:72-131, restart.f90:17-63):
  * a Fortran unformatted record with the time as a 4-byte real (12 bytes with its markers),
  * then uu(nx,ny,nz,8) as 8-byte reals in Fortran order.  laps_write_output writes the current
@@ -347,6 +356,25 @@ int laps_conv3_forward(const void* x, const void* wpk, const float* bias, void* 
 int laps_conv3_wgrad(const void* x, const void* dz, float* dw, int nx, int ny, int nz, int cin_p, int cout_p,
                      void* stream);
 int laps_conv3_status(void* stream, int* err);
+
+/* The closure's data on the device (cubic periodic grids of side 2 pi; device pointers;
+ * asynchronous on `stream`; no allocation):
+ *   laps_closure_filter: box filter of width `ratio` of a fine incompressible state
+ *     fine(n,n,n,1:8) (n = nfine, the layout of laps_state_real_device), sampled on the coarse
+ *     grid of n/ratio points: coarse(.,.,.,1:8) the filtered state; targets (float32, 12
+ *     fields) the subgrid stress tau_ij = <u_i u_j> - <u_i><u_j> - (<b_i b_j> - <b_i><b_j>)
+ *     for ij = xx xy xz yy yz zz, the subgrid electromotive force <u x b> - <u> x <b>, and 3
+ *     zero fields (the Hall part, not modelled: the training runs have d_i = 0).
+ *   laps_closure_pack_input: the net's input from a coarse state (u = rho u / rho and B,
+ *     divided by su and sb) in the convolutions' padded layout with 16 channels.
+ *   laps_closure_unpack_output: the net's 12 output channels times s into 12 float64 fields.
+ *   laps_closure_forcing: from the spectra of those 12 fields (layout of
+ *     laps_download_spectral), the closure's right-hand side of the 8 state fields: 0,
+ *     the momentum -(i k . tau) projected on k-perpendicular, the induction i k x eps, 0. */
+int laps_closure_filter(const double* fine, int nfine, int ratio, double* coarse, float* targets, void* stream);
+int laps_closure_pack_input(const double* state, void* x, int n, double su, double sb, void* stream);
+int laps_closure_unpack_output(const void* y, double* tau, int n, double s, void* stream);
+int laps_closure_forcing(const double* tau_spec, double* force_spec, int n, void* stream);
 
 /* Bounded wait for all queued work of the context. */
 int laps_wait(laps_ctx* ctx, int timeout_ms);

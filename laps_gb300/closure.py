@@ -26,6 +26,21 @@ def _lib():
         lib.laps_conv3_wgrad.argtypes = [vp, vp, vp, i, i, i, i, i, vp]
         lib.laps_conv3_status.restype = i
         lib.laps_conv3_status.argtypes = [vp, C.POINTER(i)]
+        d = C.c_double
+        lib.laps_closure_filter.restype = i
+        lib.laps_closure_filter.argtypes = [vp, i, i, vp, vp, vp]
+        lib.laps_closure_pack_input.restype = i
+        lib.laps_closure_pack_input.argtypes = [vp, vp, i, d, d, vp]
+        lib.laps_closure_unpack_output.restype = i
+        lib.laps_closure_unpack_output.argtypes = [vp, vp, i, d, vp]
+        lib.laps_closure_forcing.restype = i
+        lib.laps_closure_forcing.argtypes = [vp, vp, i, vp]
+        lib.laps_state_real_device.restype = i
+        lib.laps_state_real_device.argtypes = [vp, vp]
+        lib.laps_add_spectral_device.restype = i
+        lib.laps_add_spectral_device.argtypes = [vp, vp, d]
+        lib.laps_transform_uu_real_to_fourier_noalloc.restype = i
+        lib.laps_transform_uu_real_to_fourier_noalloc.argtypes = [vp, vp, i, i, i, i, vp]
         _bound = True
     return lib
 
@@ -152,16 +167,16 @@ class ClosureNet:
             self.pk.append(pack(w, ci, co))
             self.pkf.append(pack(w, ci, co, flip=True))
 
-    def forward(self, x):
+    def forward(self, x, keep=True):
         """x: (nz, ny, nx + 2, 16) padded BF16 input.  Returns the padded output (16 channels,
-        12 used)."""
+        12 used).  keep=False (inference) skips the pre-activations backward needs."""
         import torch
 
         self.acts, self.pre = [x], []
         a = x
         for l, (cin, cout, act) in enumerate(self.layers):
             co = padded_channels(cout)
-            z = torch.empty(a.shape[:3] + (co,), dtype=torch.bfloat16, device=a.device) if act else None
+            z = torch.empty(a.shape[:3] + (co,), dtype=torch.bfloat16, device=a.device) if act and keep else None
             a = conv3(a, self.pk[l], co, bias=self.b[l].detach(), act=act, zpre=z)
             self.pre.append(z)
             self.acts.append(a)
@@ -180,3 +195,75 @@ class ClosureNet:
                 ci = padded_channels(cin)
                 g = conv3(g, self.pkf[l], ci, act=2, gate=self.pre[l - 1])
         return g
+
+
+# ------------------------------------------------------------------------------ the study
+def state_real(run, out=None):
+    """The conserved real state of a run, (8, n, n, n) float64 on the device."""
+    import torch
+
+    nz, ny, nx = run.shape
+    out = out if out is not None else torch.empty((8, nz, ny, nx), dtype=torch.float64, device="cuda")
+    run._ck(_lib().laps_state_real_device(run.h, out.data_ptr()))
+    return out
+
+
+def filter_state(fine, ratio):
+    """Box filter + sampling of a fine (8, n, n, n) state: (coarse state (8, m, m, m) float64,
+    targets (12, m, m, m) float32), m = n / ratio."""
+    import torch
+
+    n = fine.shape[-1]
+    m = n // ratio
+    coarse = torch.empty((8, m, m, m), dtype=torch.float64, device=fine.device)
+    tgt = torch.empty((12, m, m, m), dtype=torch.float32, device=fine.device)
+    _ck(_lib().laps_closure_filter(fine.data_ptr(), n, ratio, coarse.data_ptr(), tgt.data_ptr(), _stream()))
+    return coarse, tgt
+
+
+def pack_input(state, su, sb, out=None):
+    import torch
+
+    n = state.shape[-1]
+    x = out if out is not None else torch.zeros((n, n, n + 2, 16), dtype=torch.bfloat16, device=state.device)
+    _ck(_lib().laps_closure_pack_input(state.data_ptr(), x.data_ptr(), n, su, sb, _stream()))
+    return x
+
+
+class Closure:
+    """A trained net with its normalisation: inputs u / su and b / sb, outputs times st."""
+
+    def __init__(self, net, su, sb, st):
+        self.net, self.su, self.sb, self.st = net, su, sb, st
+
+    def forcing(self, state, n):
+        """The closure's right-hand side (8 spectral fields, laps_download_spectral layout) of a
+        coarse state (8, n, n, n) on the device."""
+        import torch
+
+        lib = _lib()
+        x = pack_input(state, self.su, self.sb)
+        y = self.net.forward(x, keep=False)
+        tau = torch.empty((12, n, n, n), dtype=torch.float64, device=state.device)
+        _ck(lib.laps_closure_unpack_output(y.data_ptr(), tau.data_ptr(), n, self.st, _stream()))
+        ts = torch.empty((12, n, n, n // 2 + 1), dtype=torch.complex128, device=state.device)
+        _ck(lib.laps_transform_uu_real_to_fourier_noalloc(tau.data_ptr(), ts.data_ptr(), n, n, n, 12, _stream()))
+        f = torch.empty((8, n, n, n // 2 + 1), dtype=torch.complex128, device=state.device)
+        _ck(lib.laps_closure_forcing(ts.data_ptr(), f.data_ptr(), n, _stream()))
+        return f
+
+
+def closed_step(run, closure, n, buf=None):
+    """One step of a coarse run with the closure: the solver's step (laps_step), then the
+    closure's right-hand side of the new state added over the step's dt (operator splitting,
+    explicit), followed by the dealias mask.  Returns (time, dt, status)."""
+    import torch
+
+    t, dt, st = run.step(1)
+    if st != 0:
+        return t, dt, st
+    state = state_real(run, buf)
+    f = closure.forcing(state, n)
+    torch.cuda.current_stream().synchronize()  # the engine's stream reads f next
+    run._ck(_lib().laps_add_spectral_device(run.h, f.data_ptr(), dt))
+    return t, dt, st

@@ -1,0 +1,214 @@
+"""The learned subgrid closure, end to end on one GPU.
+
+1. Training data: fine incompressible MHD runs (random-phase 1 <= |k| <= 8 spectrum with
+   |k|^-1 amplitudes, rms u = rms b = 0.5 over B0 = (1, 0, 0), eta = nu = 5e-4, 2/3 mask),
+   advanced by this library's solver; snapshots are box-filtered to the coarse grid on the
+   device (laps_closure_filter): the filtered state is the net's input, the subgrid stress
+   and electromotive force its target.
+2. Training: the 4-layer BF16 convolution net on the tcgen05 kernels (forward, input and
+   weight gradients), Adam on FP32 master weights, mean squared error of the normalised
+   targets.
+3. Evaluation: from the filtered state of a held-out seed's fine run, a coarse run with the
+   closure (its right-hand side added over each step) and one without it advance to the fine
+   run's final time; their shell energy spectra E(k) = E_u + E_b for k <= k_cut are compared
+   with the filtered fine run's.  The closed run is selected when its largest relative
+   spectrum error is below the threshold and below the unclosed run's; otherwise the unclosed
+   run is the fallback.  Wall times of the fine and the closed runs over the interval are
+   reported.
+
+The Hall term and the expanding box are off in these runs (the filter's Hall target is zero).
+``python -m laps_gb300.closure_study`` prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+KW = dict(if_resis=1, resistivity=5e-4, if_visc=1, viscosity=5e-4, dealias_option=1, cfl=0.4, rho0=1.0)
+
+
+def _fine_run(ffi, n, seed, prec):
+    from .ic import turbulence_ic
+
+    prim = turbulence_ic(n, kmin=1, kmax=8, alpha=-1.0, rms_u=0.5, rms_b=0.5, seed=seed, p0=1.0)
+    g = ffi.Laps(ffi.params(nx=n, ny=n, nz=n, variant=ffi.VARIANT_3DI, precision=prec, **KW))
+    g.upload_state(prim, primitive=True)
+    g.set_time(0.0)
+    return g
+
+
+def _coarse_run(ffi, state, t0, prec):
+    n = state.shape[-1]
+    g = ffi.Laps(ffi.params(nx=n, ny=n, nz=n, variant=ffi.VARIANT_3DI, precision=prec, **KW))
+    g.upload_state(np.ascontiguousarray(state.cpu().numpy()), primitive=False)
+    g.set_time(t0)
+    return g
+
+
+def _spectrum(g, nshell):
+    eu, eb = g.spectrum(nshell)
+    return eu + eb
+
+
+def dataset(ffi, closure, seeds, n_fine, ratio, warm, snaps, every, prec):
+    """(inputs: coarse states (8, m, m, m) float64, targets (12, m, m, m) float32) per snapshot."""
+    import torch
+
+    states, targets = [], []
+    buf = torch.empty((8, n_fine, n_fine, n_fine), dtype=torch.float64, device="cuda")
+    for seed in seeds:
+        g = _fine_run(ffi, n_fine, seed, prec)
+        g.step(warm)
+        for _ in range(snaps):
+            g.step(every)
+            c, t = closure.filter_state(closure.state_real(g, buf), ratio)
+            states.append(c)
+            targets.append(t)
+        g.close()
+    del buf
+    torch.cuda.empty_cache()
+    return states, targets
+
+
+def train(closure, states, targets, iters, lr, seed=0):
+    import torch
+
+    rms = lambda ts: float(torch.sqrt(torch.stack([t.pow(2).mean() for t in ts]).mean()))
+    su = rms([s[1:4] / s[0:1] for s in states])
+    sb = rms([s[4:7] for s in states])
+    st = rms([t[:9] for t in targets])
+    xs = [closure.pack_input(s, su, sb) for s in states]
+    ys = [t / st for t in targets]
+    net = closure.ClosureNet(device="cuda", seed=seed)
+    opt = torch.optim.Adam(net.parameters(), lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, iters)
+    rng = np.random.default_rng(seed)
+    losses = []
+    for it in range(iters):
+        i = int(rng.integers(len(xs)))
+        y = net.forward(xs[i])
+        r = closure.from_padded(y, 12) - ys[i]
+        losses.append(float((r ** 2).mean()))
+        net.backward(closure.to_padded(2 * r / r.numel()))
+        opt.step()
+        sched.step()
+        net.repack()
+    if closure.status() != 0:
+        raise RuntimeError("a convolution's bounded wait ran out during training")
+    return closure.Closure(net, su, sb, st), losses
+
+
+def a_priori(model, states, targets):
+    """Correlation of predicted and filtered subgrid terms (stress 0..5, EMF 6..8)."""
+    import torch
+
+    from . import closure
+
+    cs, ce = [], []
+    for s, t in zip(states, targets):
+        y = closure.from_padded(model.net.forward(closure.pack_input(s, model.su, model.sb), keep=False), 12) * model.st
+        for grp, out in ((slice(0, 6), cs), (slice(6, 9), ce)):
+            a, b = y[grp].flatten().double(), t[grp].flatten().double()
+            out.append(float(torch.corrcoef(torch.stack([a, b]))[0, 1]))
+    return {"stress_corr": float(np.mean(cs)), "emf_corr": float(np.mean(ce))}
+
+
+def main(argv=None):
+    import torch
+
+    from . import closure, ffi
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--fine", type=int, default=512)
+    ap.add_argument("--ratio", type=int, default=4)
+    ap.add_argument("--train-seeds", default="10,11,12,13")
+    ap.add_argument("--eval-seed", type=int, default=20)
+    ap.add_argument("--warm", type=int, default=150)
+    ap.add_argument("--snaps", type=int, default=10)
+    ap.add_argument("--every", type=int, default=15)
+    ap.add_argument("--iters", type=int, default=600)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--eval-steps", type=int, default=150, help="fine steps of the evaluation interval")
+    ap.add_argument("--threshold", type=float, default=0.05)
+    args = ap.parse_args(argv)
+    prec_fine, prec_coarse = ffi.PREC_FP32_F64, ffi.PREC_FP64
+    n = args.fine // args.ratio
+    t0 = time.perf_counter()
+    states, targets = dataset(ffi, closure, [int(s) for s in args.train_seeds.split(",")], args.fine, args.ratio,
+                              args.warm, args.snaps, args.every, prec_fine)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    model, losses = train(closure, states, targets, args.iters, args.lr)
+    t_train = time.perf_counter() - t0
+    del states, targets
+    torch.cuda.empty_cache()
+    # held-out seed: a-priori test on its snapshots, then the a-posteriori runs
+    ev_states, ev_targets = dataset(ffi, closure, [args.eval_seed], args.fine, args.ratio, args.warm, 2, args.every,
+                                    prec_fine)
+    prior = a_priori(model, ev_states, ev_targets)
+    del ev_states, ev_targets
+    fine = _fine_run(ffi, args.fine, args.eval_seed, prec_fine)
+    fine.step(args.warm)
+    buf = torch.empty((8, args.fine, args.fine, args.fine), dtype=torch.float64, device="cuda")
+    c0, _ = closure.filter_state(closure.state_real(fine, buf), args.ratio)
+    t_start, _ = fine.time()
+    fine.wait()
+    w0 = time.perf_counter()
+    t_end, _, st_f = fine.step(args.eval_steps)
+    fine.wait()
+    wall_fine = time.perf_counter() - w0
+    cf, _ = closure.filter_state(closure.state_real(fine, buf), args.ratio)
+    fine.close()
+    del buf
+    torch.cuda.empty_cache()
+    nshell = n // 2 + 1
+    kcut = n // 4  # k <= k_max / 2 with k_max = n / 3 of the 2/3 mask, rounded down: n / 4 = 32 at 128^3
+    ref = _coarse_run(ffi, cf, t_end, prec_coarse)
+    e_ref = _spectrum(ref, nshell)
+    ref.close()
+    runs = {}
+    for name in ("closed", "unclosed"):
+        g = _coarse_run(ffi, c0, t_start, prec_coarse)
+        sbuf = torch.empty((8, n, n, n), dtype=torch.float64, device="cuda")
+        steps, t, st = 0, t_start, 0
+        g.wait()
+        w0 = time.perf_counter()
+        while t < t_end and st == 0 and steps < 100000:
+            if name == "closed":
+                t, dt, st = closure.closed_step(g, model, n, sbuf)
+            else:
+                t, dt, st = g.step(1)
+            steps += 1
+        g.wait()
+        wall = time.perf_counter() - w0
+        e = _spectrum(g, nshell)
+        rel = np.abs(e[1:kcut + 1] - e_ref[1:kcut + 1]) / np.maximum(e_ref[1:kcut + 1], 1e-300)
+        d = g.diagnostics()
+        runs[name] = {"steps": steps, "time": t, "status": st, "wall_s": wall, "spectrum_max_rel_err": float(rel.max()),
+                      "spectrum_mean_rel_err": float(rel.mean()),
+                      "spectrum_rel_err_by_shell": [float(f"{v:.3g}") for v in rel], "e_kin": d.e_kin,
+                      "e_mag": d.e_mag}
+        g.close()
+    ok = runs["closed"]["spectrum_max_rel_err"] <= args.threshold and \
+        runs["closed"]["spectrum_max_rel_err"] <= runs["unclosed"]["spectrum_max_rel_err"]
+    out = {
+        "study": "learned subgrid closure", "fine": f"{args.fine}^3", "coarse": f"{n}^3",
+        "train_seeds": args.train_seeds, "eval_seed": args.eval_seed, "samples": args.snaps * len(args.train_seeds.split(",")),
+        "data_s": t_data, "train_s": t_train, "iters": args.iters,
+        "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])), "a_priori": prior,
+        "interval": {"t_start": t_start, "t_end": t_end, "fine_steps": args.eval_steps, "fine_status": st_f,
+                     "fine_wall_s": wall_fine},
+        "k_cut": kcut, "threshold": args.threshold, "runs": runs,
+        "selected": "closed" if ok else "unclosed (fallback)",
+        "speedup_closed_vs_fine": wall_fine / runs["closed"]["wall_s"],
+    }
+    print(json.dumps(out), flush=True)
+    return out
+
+
+if __name__ == "__main__":
+    main()

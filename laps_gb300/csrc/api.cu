@@ -221,6 +221,14 @@ int laps_calc_rhs(laps_ctx* c, double* fnl) {
   return guarded(c, [&] { c->e->calc_rhs(fnl); });
 }
 int laps_dealias(laps_ctx* c) { return guarded(c, [&] { c->e->dealias_state(); }); }
+int laps_state_real_device(laps_ctx* c, double* uu_dev) {
+  if (!uu_dev) return fail(c, LAPS_EINVAL, "null buffer");
+  return guarded(c, [&] { c->e->state_real_device(uu_dev); });
+}
+int laps_add_spectral_device(laps_ctx* c, const double* duf_dev, double scale) {
+  if (!duf_dev) return fail(c, LAPS_EINVAL, "null buffer");
+  return guarded(c, [&] { c->e->add_spectral_device(duf_dev, scale); });
+}
 int laps_transform_uu_k2r(laps_ctx* c, double* uu) {
   if (!uu) return fail(c, LAPS_EINVAL, "null output");
   return guarded(c, [&] { c->e->download(uu, nullptr); });

@@ -497,6 +497,170 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------- closure data
+// Subgrid quantities of the incompressible run: a box filter of width r (fine n_f = r n_c)
+// followed by sampling on the coarse grid.  Per coarse voxel, with u = (rho u) / rho and b = B:
+//   coarse state  (rho, rho u, B, p) box means (reference order, 8 fields)
+//   targets 0..5  tau_ij = <u_i u_j> - <u_i><u_j> - (<b_i b_j> - <b_i><b_j>), ij = xx xy xz yy yz zz
+//                 (the symmetric Reynolds-minus-Maxwell stress the coarse momentum misses)
+//   targets 6..8  eps = <u x b> - <u> x <b> (the subgrid electromotive force)
+//   targets 9..11 the Hall part of the subgrid electromotive force: zero (the runs this
+//                 filter serves have d_i = 0)
+__global__ void k_closure_filter(const double* __restrict__ fine, int nf, int r, double* __restrict__ coarse,
+                                 float* __restrict__ tgt) {
+  const int nc = nf / r;
+  const long long ncell = (long long)nc * nc * nc, nfp = (long long)nf * nf * nf;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    const int cx = (int)(c % nc), cy = (int)((c / nc) % nc), cz = (int)(c / ((long long)nc * nc));
+    double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // means of the 8 state fields
+    double su[3] = {0, 0, 0}, sb[3] = {0, 0, 0}, uu[6] = {0, 0, 0, 0, 0, 0}, bb[6] = {0, 0, 0, 0, 0, 0}, ub[3] = {0, 0, 0};
+    for (int dz = 0; dz < r; dz++)
+      for (int dy = 0; dy < r; dy++)
+        for (int dx = 0; dx < r; dx++) {
+          const long long i = ((long long)(cz * r + dz) * nf + (cy * r + dy)) * nf + (cx * r + dx);
+          double q[8];
+#pragma unroll
+          for (int f = 0; f < 8; f++) {
+            q[f] = fine[f * nfp + i];
+            m[f] += q[f];
+          }
+          const double u[3] = {q[1] / q[0], q[2] / q[0], q[3] / q[0]}, b[3] = {q[4], q[5], q[6]};
+          int k = 0;
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            su[a] += u[a];
+            sb[a] += b[a];
+#pragma unroll
+            for (int e = a; e < 3; e++, k++) {
+              uu[k] += u[a] * u[e];
+              bb[k] += b[a] * b[e];
+            }
+          }
+          ub[0] += u[1] * b[2] - u[2] * b[1];
+          ub[1] += u[2] * b[0] - u[0] * b[2];
+          ub[2] += u[0] * b[1] - u[1] * b[0];
+        }
+    const double w = 1.0 / ((double)r * r * r);
+#pragma unroll
+    for (int f = 0; f < 8; f++) coarse[f * ncell + c] = m[f] * w;
+    double ua[3], ba[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      ua[a] = su[a] * w;
+      ba[a] = sb[a] * w;
+    }
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int e = a; e < 3; e++, k++)
+        tgt[k * ncell + c] = (float)((uu[k] * w - ua[a] * ua[e]) - (bb[k] * w - ba[a] * ba[e]));
+    tgt[6 * ncell + c] = (float)(ub[0] * w - (ua[1] * ba[2] - ua[2] * ba[1]));
+    tgt[7 * ncell + c] = (float)(ub[1] * w - (ua[2] * ba[0] - ua[0] * ba[2]));
+    tgt[8 * ncell + c] = (float)(ub[2] * w - (ua[0] * ba[1] - ua[1] * ba[0]));
+    for (int f = 9; f < 12; f++) tgt[f * ncell + c] = 0.0f;
+  }
+}
+
+// the net's input from a coarse state (8 fields): u = (rho u) / rho and B, divided by su and
+// sb, in the convolutions' padded layout (16 channels, 6 used, x halo)
+__global__ void k_closure_pack_input(const double* __restrict__ st, __nv_bfloat16* __restrict__ x, int n, double su, double sb) {
+  const long long np = (long long)n * n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % n);
+    const long long row = i / n;
+    const double rho = st[i];
+    __align__(16) __nv_bfloat16 v[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) v[c] = __float2bfloat16_rn(0.0f);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      v[a] = __float2bfloat16_rn((float)(st[(1 + a) * np + i] / rho / su));
+      v[3 + a] = __float2bfloat16_rn((float)(st[(4 + a) * np + i] / sb));
+    }
+    const long long o = (row * (n + 2) + ix + 1) * 16;
+    reinterpret_cast<uint4*>(x + o)[0] = reinterpret_cast<const uint4*>(v)[0];
+    reinterpret_cast<uint4*>(x + o)[1] = reinterpret_cast<const uint4*>(v)[1];
+    if (ix == 0 || ix == n - 1) {
+      const long long h = (row * (n + 2) + (ix == 0 ? n + 1 : 0)) * 16;
+      reinterpret_cast<uint4*>(x + h)[0] = reinterpret_cast<const uint4*>(v)[0];
+      reinterpret_cast<uint4*>(x + h)[1] = reinterpret_cast<const uint4*>(v)[1];
+    }
+  }
+}
+
+// the net's output (padded layout, 16 channels, 12 used) times s -> 12 real FP64 fields
+__global__ void k_closure_unpack(const __nv_bfloat16* __restrict__ y, double* __restrict__ tau, int n, double s) {
+  const long long np = (long long)n * n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
+    const long long o = ((i / n) * (n + 2) + i % n + 1) * 16;
+    __align__(16) __nv_bfloat16 v[16];
+    reinterpret_cast<uint4*>(v)[0] = reinterpret_cast<const uint4*>(y + o)[0];
+    reinterpret_cast<uint4*>(v)[1] = reinterpret_cast<const uint4*>(y + o)[1];
+#pragma unroll
+    for (int c = 0; c < 12; c++) tau[c * np + i] = s * (double)__bfloat162float(v[c]);
+  }
+}
+
+// The closure's right-hand side in Fourier space (periodic box of side 2 pi, wave numbers m
+// with the Nyquist index at +n/2 as the solver's): from the subgrid stress and electromotive
+// force spectra (12 fields, laps_download_spectral layout),
+//   momentum  f = -(i k . tau), projected on k-perpendicular (the incompressible solver's
+//             pressure projection; 0 at k = 0)
+//   induction g = i k x (eps + eps_Hall)
+// into the 8 state fields (rho, rho u, B, p): 0, f, g, 0.
+__global__ void k_closure_forcing(const double2* __restrict__ ts, double2* __restrict__ out, int n) {
+  const int nh = n / 2 + 1;
+  const long long ns = (long long)nh * n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ns; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % nh), iy = (int)((i / nh) % n), iz = (int)(i / ((long long)nh * n));
+    const double k[3] = {(double)ix, (double)(iy <= n / 2 ? iy : iy - n), (double)(iz <= n / 2 ? iz : iz - n)};
+    double2 t[12];
+#pragma unroll
+    for (int c = 0; c < 12; c++) t[c] = ts[c * ns + i];
+    // tau rows: (xx xy xz), (xy yy yz), (xz yz zz)
+    const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    double2 f[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      double re = 0, im = 0;  // -i k_j tau_aj
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        re += k[j] * t[idx[a][j]].y;
+        im -= k[j] * t[idx[a][j]].x;
+      }
+      f[a] = make_double2(re, im);
+    }
+    const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    if (k2 > 0.0) {
+      const double dre = (k[0] * f[0].x + k[1] * f[1].x + k[2] * f[2].x) / k2;
+      const double dim = (k[0] * f[0].y + k[1] * f[1].y + k[2] * f[2].y) / k2;
+#pragma unroll
+      for (int a = 0; a < 3; a++) f[a] = make_double2(f[a].x - k[a] * dre, f[a].y - k[a] * dim);
+    } else {
+      f[0] = f[1] = f[2] = make_double2(0.0, 0.0);
+    }
+    double2 e[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) e[a] = make_double2(t[6 + a].x + t[9 + a].x, t[6 + a].y + t[9 + a].y);
+    // i (k x e): component a = i (k_b e_c - k_c e_b)
+    double2 g[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const int b = (a + 1) % 3, c = (a + 2) % 3;
+      const double cre = k[b] * e[c].x - k[c] * e[b].x, cim = k[b] * e[c].y - k[c] * e[b].y;
+      g[a] = make_double2(-cim, cre);
+    }
+    out[i] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      out[(1 + a) * ns + i] = f[a];
+      out[(4 + a) * ns + i] = g[a];
+    }
+    out[7 * ns + i] = make_double2(0.0, 0.0);
+  }
+}
+
 // Packed weights of one layer, bf16 [tap][K chunk][N row][8], from fp32 w[co][ci][kz][ky][kx]
 // (torch's Conv3d order; tap = (kz * 3 + ky) * 3 + kx; the layer computes the cross-correlation
 // out[x] = sum w[k] in[x + k - 1]).  flip != 0 packs the weights of the input-gradient
@@ -672,6 +836,71 @@ extern "C" int laps_conv3_wgrad(const void* x, const void* dz, float* dw, int nx
     else launch_wgrad<16, 16>(s, x, dz, dw, nx, ny, nz, err);
   } catch (const Error& e) {
     laps_set_create_error("conv3 wgrad: " + e.msg);
+    return e.code;
+  }
+  return LAPS_OK;
+}
+
+extern "C" int laps_closure_filter(const double* fine, int nfine, int ratio, double* coarse, float* targets, void* stream) {
+  using namespace laps;
+  if (!fine || !coarse || !targets || ratio < 1 || nfine < ratio || nfine % ratio) {
+    laps_set_create_error("closure filter: null buffer or the fine size not a multiple of the ratio");
+    return LAPS_EINVAL;
+  }
+  try {
+    k_closure_filter<<<4 * 152, 256, 0, (cudaStream_t)stream>>>(fine, nfine, ratio, coarse, targets);
+    LAPS_CK(cudaGetLastError());
+  } catch (const Error& e) {
+    laps_set_create_error("closure filter: " + e.msg);
+    return e.code;
+  }
+  return LAPS_OK;
+}
+
+extern "C" int laps_closure_pack_input(const double* state, void* x, int n, double su, double sb, void* stream) {
+  using namespace laps;
+  if (!state || !x || n < 2 || !conv_aligned(x) || su <= 0 || sb <= 0) {
+    laps_set_create_error("closure pack: bad argument");
+    return LAPS_EINVAL;
+  }
+  try {
+    k_closure_pack_input<<<4 * 152, 256, 0, (cudaStream_t)stream>>>(state, reinterpret_cast<__nv_bfloat16*>(x), n, su, sb);
+    LAPS_CK(cudaGetLastError());
+  } catch (const Error& e) {
+    laps_set_create_error("closure pack: " + e.msg);
+    return e.code;
+  }
+  return LAPS_OK;
+}
+
+extern "C" int laps_closure_unpack_output(const void* y, double* tau, int n, double s, void* stream) {
+  using namespace laps;
+  if (!y || !tau || n < 2 || !conv_aligned(y)) {
+    laps_set_create_error("closure unpack: bad argument");
+    return LAPS_EINVAL;
+  }
+  try {
+    k_closure_unpack<<<4 * 152, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const __nv_bfloat16*>(y), tau, n, s);
+    LAPS_CK(cudaGetLastError());
+  } catch (const Error& e) {
+    laps_set_create_error("closure unpack: " + e.msg);
+    return e.code;
+  }
+  return LAPS_OK;
+}
+
+extern "C" int laps_closure_forcing(const double* tau_spec, double* force_spec, int n, void* stream) {
+  using namespace laps;
+  if (!tau_spec || !force_spec || n < 2 || (n & (n - 1))) {
+    laps_set_create_error("closure forcing: bad argument");
+    return LAPS_EINVAL;
+  }
+  try {
+    k_closure_forcing<<<4 * 152, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const double2*>(tau_spec),
+                                                                reinterpret_cast<double2*>(force_spec), n);
+    LAPS_CK(cudaGetLastError());
+  } catch (const Error& e) {
+    laps_set_create_error("closure forcing: " + e.msg);
     return e.code;
   }
   return LAPS_OK;

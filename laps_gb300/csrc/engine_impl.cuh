@@ -108,6 +108,10 @@ class EngineBase {
   virtual long long grid_points() const = 0;
   virtual int variant() const = 0;
   virtual const laps_params& params() const = 0;
+  // device-side exchange with a caller (the closure): the 8 conserved real fields into a
+  // device buffer; U += scale * duf (reference spectral layout, 8 fields) then the dealias
+  virtual void state_real_device(double* dst) = 0;
+  virtual void add_spectral_device(const double* duf, double scale) = 0;
   // granular, unfused path (bisection against the reference's subroutines)
   virtual void calc_flux(double* host, int spectral) = 0;
   virtual void calc_rhs(double* host) = 0;
@@ -892,6 +896,17 @@ template <class T, class TS = T> class Engine : public EngineBase {
                                                      P.variant == LAPS_VARIANT_3DI);
     LAPS_CK(cudaGetLastError());
     return out;
+  }
+  void state_real_device(double* dst) override {
+    const double* rs = stage_real_state();
+    LAPS_CK(cudaMemcpyAsync(dst, rs, 8 * gfull.fsr * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    wait(tmo());
+  }
+  void add_spectral_device(const double* duf, double scale) override {
+    if (!have_state) throw Error{LAPS_ESTATE, "no state uploaded"};
+    k_spec_axpy_ref<TS><<<1024, 256, 0, stream>>>((const double2*)duf, B.U, gfull, 8, scale);
+    LAPS_CK(cudaGetLastError());
+    dealias_state();  // (waits)
   }
   void angle_statistics(int axis, double* hout) override {
     const double* rs = stage_real_state();  // 8 conserved fields, then ux, uy, uz, p

@@ -387,6 +387,20 @@ __global__ void k_spec_from_ref(const double2* __restrict__ in, typename Store<T
   }
 }
 
+// U += scale * in for nf fields, `in` in the reference's (nx/2+1, ny, nz) complex layout
+template <class T>
+__global__ void k_spec_axpy_ref(const double2* __restrict__ in, typename Store<T>::C* U, Geo g, int nf, double scale) {
+  long long tot = (long long)nf * g.nz * g.ny * g.nh;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % g.nh);
+    const long long r = i / g.nh;
+    typename Store<T>::C* u = U + r * g.kxp + kx;
+    const double2 d = in[i];
+    const cx<T> v = Store<T>::ldc(u);
+    Store<T>::stc(u, v + cx<T>{Real<T>::from_d(scale * d.x), Real<T>::from_d(scale * d.y)});
+  }
+}
+
 // --------------------------------------------------------------------------- tables / scalars
 // Rebuild the wave-number tables for radius R (evolve_radius / update_ksquare,
 // AEBmod.f90:56-73,87-125; derivative factors of mhdrhs.f90:191-204).
