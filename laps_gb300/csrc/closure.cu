@@ -15,11 +15,13 @@
 // by choosing the source row, x by the halo.  C (the padded channel count) is 16 or 32.
 //
 // Shared memory holds all 27 taps of the packed weights for the whole kernel and a ring of
-// activation stages, one per tap.  Operand layout in shared memory (no swizzle, K-major):
-// core matrices of 8 rows x 16 bytes stored contiguously; for A (a tap's 128 voxels x C
-// channels) chunk k of 8 channels is one 2 KB TMA box, so core matrices adjacent in M are
-// 128 B apart and those adjacent in K 2048 B apart; the packed weights of a tap are
-// [K chunk][N rows][8], N-adjacent 128 B apart, K-adjacent N * 16 B apart.
+// activation stages, one per (dz, dy): the 130 voxels x0 - 1 .. x0 + 128 of the source row,
+// which serve the three dx taps.  Operand layout in shared memory (no swizzle, K-major): core
+// matrices of 8 rows x 16 bytes stored contiguously and one after the other along M, so every
+// row lies 16 bytes after the previous one and the operand of tap dx is the same stage with
+// its start moved by dx rows; chunk k of 8 channels is one TMA box of 130 rows (2080 B), so
+// core matrices adjacent in M are 128 B apart and those adjacent in K 2080 B apart.  The packed
+// weights of a tap are [K chunk][N rows][8], N-adjacent 128 B apart, K-adjacent N * 16 B apart.
 //
 // Roles (192 threads, persistent over tiles): warp 0 issues the TMA loads, warp 1 allocates
 // tensor memory and issues the MMAs, warps 2-5 read the accumulator back (tcgen05.ld; warp w
@@ -132,8 +134,9 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 template <int KC, int NP> struct ConvCfg {
-  static constexpr int A_CHUNK = CONV_TILE * 16;              // 8 channels of 128 voxels
-  static constexpr int A_BYTES = KC * A_CHUNK;                // one tap
+  static constexpr int A_ROWS = CONV_TILE + 2;                // x0 - 1 .. x0 + 128: the three dx taps
+  static constexpr int A_CHUNK = A_ROWS * 16;                 // 8 channels of those voxels
+  static constexpr int A_BYTES = KC * A_CHUNK;                // one (dz, dy) stage
   static constexpr int B_TAP = KC * NP * 16;                  // one tap of packed weights
   static constexpr int B_BYTES = 27 * B_TAP;
   // an operand read with its two strides exchanged would reach 16 x 2 KB past a stage's start:
@@ -197,15 +200,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       for (int tile = blockIdx.x; tile < a.ntiles && !bail; tile += gridDim.x) {
         const int x0 = (tile % xt) * CONV_TILE;
         const int r = tile / xt, y = r % a.ny, z = r / a.ny;
-        for (int t = 0; t < 27; t++) {
+        for (int t = 0; t < 9; t++) {  // one stage per (dz, dy): the rows of all three dx taps
           if (!conv_wait(&empty[s], ph ^ 1u)) {
             bail = 1;
             atomicExch(a.err, 1);
             break;
           }
-          const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+          const int dz = t / 3, dy = t % 3;
           const int zz = (z + dz - 1 + a.nz) % a.nz, yy = (y + dy - 1 + a.ny) % a.ny;
-          const int row = (zz * a.ny + yy) * pitch + x0 + dx;
+          const int row = (zz * a.ny + yy) * pitch + x0;
           mbar_arrive_expect_tx(&full[s], CF::A_BYTES);
 #pragma unroll
           for (int k = 0; k < KC; k++) tma_load_2d(A + s * CF::A_BYTES + k * CF::A_CHUNK, &tx, k * 8, row, &full[s]);
@@ -236,18 +239,22 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
         tc_fence_after();
         const uint32_t d = tbase + acc * NP;
         bool ok = true;
-        for (int t = 0; t < 27; t++) {
+        for (int t = 0; t < 9; t++) {
           if (!conv_wait(&full[s], ph)) {
             ok = false;
             break;
           }
           tc_fence_after();
+          // rows lie 16 bytes apart (core matrices of 8 rows are contiguous), so the operand of
+          // tap dx starts dx rows into the stage
 #pragma unroll
-          for (int j = 0; j < KC / 2; j++) {
-            const uint64_t ad = smem_desc(A + s * CF::A_BYTES + 2 * j * CF::A_CHUNK, CF::A_CHUNK, 128);
-            const uint64_t bd = smem_desc(B + t * CF::B_TAP + 2 * j * NP * 16, NP * 16, 128);
-            umma_bf16(d, ad, bd, IDESC, (t | j) != 0);
-          }
+          for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+            for (int j = 0; j < KC / 2; j++) {
+              const uint64_t ad = smem_desc(A + s * CF::A_BYTES + 2 * j * CF::A_CHUNK + dx * 16, CF::A_CHUNK, 128);
+              const uint64_t bd = smem_desc(B + (3 * t + dx) * CF::B_TAP + 2 * j * NP * 16, NP * 16, 128);
+              umma_bf16(d, ad, bd, IDESC, (t | dx | j) != 0);
+            }
           umma_commit(&empty[s]);  // the stage is free once these MMAs have read it
           if (++s == CONV_STAGES) {
             s = 0;
@@ -705,6 +712,7 @@ static void launch_conv3(cudaStream_t s, const void* x, const void* wpk, ConvArg
   using CF = ConvCfg<KC, NP>;
   auto kern = k_conv3<KC, NP>;
   LAPS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
+  LAPS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
   LAPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CONV_THREADS, CF::SMEM));
   int dev = 0, nsm = 0;
@@ -712,7 +720,7 @@ static void launch_conv3(cudaStream_t s, const void* x, const void* wpk, ConvArg
   LAPS_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   if (per_sm < 1) throw Error{LAPS_ECUDA, "conv kernel does not fit on an SM"};
   const int grid = a.ntiles < nsm * per_sm ? a.ntiles : nsm * per_sm;
-  const CUtensorMap tm = conv_tensor_map(x, (long long)a.nz * a.ny * (a.nx + 2), KC * 8);
+  const CUtensorMap tm = conv_tensor_map_box(x, (long long)a.nz * a.ny * (a.nx + 2), KC * 8, CF::A_ROWS);
   kern<<<grid, CONV_THREADS, CF::SMEM, s>>>(tm, reinterpret_cast<const uint4*>(wpk), a);
   LAPS_CK(cudaGetLastError());
 }
@@ -722,6 +730,7 @@ static void launch_wgrad(cudaStream_t s, const void* x, const void* dz, float* d
   using CF = WgCfg<CI, NP>;
   auto kern = k_conv3_wgrad<CI, NP, LAPS_WGRAD_SWAP>;
   LAPS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
+  LAPS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int dev = 0, nsm = 0;
   LAPS_CK(cudaGetDevice(&dev));
   LAPS_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

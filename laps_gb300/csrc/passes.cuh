@@ -1193,6 +1193,9 @@ __global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, Pass
   using CS = typename Store<TS>::C;
   const Geo& g = a.g;
   const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
+  constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
+  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
+  const float tsf = (float)a.st->ts[a.stage], rrf = (float)a.st->r_ratio;
   const long long nkx = g.kx_keep, nky = g.nky();
   const long long tot = nkx * nky * g.nkz();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
@@ -1202,11 +1205,23 @@ __global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, Pass
     const long long idx = ((long long)kz * g.ny + ky) * g.kxp + kx;
     const cx<TS> m1 = Store<TS>::ldc(b.U + 1 * g.fsc + idx), m2 = Store<TS>::ldc(b.U + 2 * g.fsc + idx),
                  m3 = Store<TS>::ldc(b.U + 3 * g.fsc + idx);
-    const cx<TS> u0 = Store<TS>::ldc(b.U + idx), r0 = rk.r_of(b.R + idx);
-    TS ax, ay, az;
-    kfac(kk.KS, a.P, kk.ps, rk.rr, kx, ky, kz, ax, ay, az);
-    const cx<TS> fnl = -((mul_i(m1, ax) + mul_i(m2, ay)) + mul_i(m3, az));
-    rk.update(0, fnl, u0, r0, b.U + idx, b.R + idx, kk.ps.zero, kx, ky, kz);
+    const cx<TS> u0 = Store<TS>::ldc(b.U + idx);
+    if constexpr (F32INC) {
+      // the right-hand side in FP32 (the mass flux's transform is FP32 in this mode), the
+      // accumulation in the state type (RkCtx::update_f32)
+      const cx<float> r0 = a.stage > 0 ? Store<T>::ldc(b.R + idx) : cx_zero<float>();
+      float ax, ay, az;
+      kfac(kk.K, a.P, kk.pc, rrf, kx, ky, kz, ax, ay, az);
+      const cx<float> fm1 = IncCvt<TS>::to_f32(m1), fm2 = IncCvt<TS>::to_f32(m2), fm3 = IncCvt<TS>::to_f32(m3);
+      const cx<float> fnl = -((mul_i(fm1, ax) + mul_i(fm2, ay)) + mul_i(fm3, az));
+      rk.update_f32(0, fnl, u0, r0, b.U + idx, b.R + idx, 0.0f, kx, ky, kz, kk.pc, ccf, ddcf, itf, tsf);
+    } else {
+      const cx<TS> r0 = rk.r_of(b.R + idx);
+      TS ax, ay, az;
+      kfac(kk.KS, a.P, kk.ps, rk.rr, kx, ky, kz, ax, ay, az);
+      const cx<TS> fnl = -((mul_i(m1, ax) + mul_i(m2, ay)) + mul_i(m3, az));
+      rk.update(0, fnl, u0, r0, b.U + idx, b.R + idx, kk.ps.zero, kx, ky, kz);
+    }
   }
 }
 
