@@ -1265,6 +1265,11 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
   using CS = typename Store<TS>::C;
   const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
   const T rr = Real<T>::from_d(a.st->r_ratio);
+  // FP32 transforms with a wider state: FP32 increments and k^2 (RkCtx::update_f32)
+  constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
+  const RkCtx<T, T> rkf = rk_ctx<T>(a, kk.pc, kk.K);
+  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
+  const float tsf = (float)a.st->ts[a.stage];
 #pragma unroll 1
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
@@ -1274,11 +1279,28 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
       cx<T> w = Store<T>::ldc(x.at(bi, m));
       return cx<T>{Real<T>::mul_pow2(w.re, sexp), Real<T>::mul_pow2(w.im, sexp)};
     };
-    TS k2 = rk.k2(kx, ky, kz);
+    TS k2 = kk.ps.zero;
+    T k2t;
+    if constexpr (F32INC) {
+      k2t = rkf.k2(kx, ky, kz);
+    } else {
+      k2 = rk.k2(kx, ky, kz);
+      k2t = Cvt<T, TS>::r(k2);
+    }
+    // the update of variable v from its right-hand side fnl and its state value u
+    auto upd = [&](int v, cx<T> fnl, cx<TS> u) {
+      CS* U = b.U + v * g.fsc + col + idx;
+      C* R = b.R + v * g.fsc + col + idx;
+      if constexpr (F32INC) {
+        const cx<float> r = a.stage > 0 ? Store<T>::ldc(R) : cx_zero<float>();
+        rk.update_f32(v, fnl, u, r, U, R, k2t, kx, ky, kz, pc, ccf, ddcf, itf, tsf);
+      } else {
+        rk.update(v, cvtc<TS>(fnl), u, U, R, k2, kx, ky, kz);
+      }
+    };
     if (grp == 0) {
       T ax, ay, az;
       kfac(K, a.P, pc, rr, kx, ky, kz, ax, ay, az);
-      const T k2t = Cvt<T, TS>::r(k2);
       cx<T> f0 = val(0), f1 = val(1), f2 = val(2);
       const bool small = Real<T>::lead(k2t) < 1e-10f;
       cx<T> kdot = cx_zero<T>();
@@ -1288,13 +1310,12 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
       }
       const cx<T> fm[3] = {small ? cx_zero<T>() : f0 + mul_i(kdot, ax), small ? cx_zero<T>() : f1 + mul_i(kdot, ay),
                            small ? cx_zero<T>() : f2 + mul_i(kdot, az)};
-      for (int v = 0; v < 4; v++) {
-        CS* U = b.U + v * g.fsc + col + idx;
-        rk.update(v, v == 0 ? cx_zero<TS>() : cvtc<TS>(fm[v - 1]), Store<TS>::ldc(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky,
-                  kz);
-      }
-      CS* U = b.U + 7 * g.fsc + col + idx;  // the new pressure replaces slot 8 before the update
-      rk.update(7, cx_zero<TS>(), cvtc<TS>(-kdot), U, b.R + 7 * g.fsc + col + idx, k2, kx, ky, kz);
+      for (int v = 0; v < 4; v++) upd(v, v == 0 ? cx_zero<T>() : fm[v - 1], Store<TS>::ldc(b.U + v * g.fsc + col + idx));
+      // the new pressure replaces slot 8 before the update
+      cx<TS> pn;
+      if constexpr (F32INC) pn = IncCvt<TS>::from_f32(-kdot);
+      else pn = cvtc<TS>(-kdot);
+      upd(7, cx_zero<T>(), pn);
     } else {
       const int v = 3 + grp;
       cx<T> f = val(0);
@@ -1302,8 +1323,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
         cx<T> w = mul_i(val(1), K.kzd[kz]);
         f = v == 4 ? f + w : f - w;
       }
-      CS* U = b.U + v * g.fsc + col + idx;
-      rk.update(v, cvtc<TS>(f), Store<TS>::ldc(U), U, b.R + v * g.fsc + col + idx, k2, kx, ky, kz);
+      upd(v, f, Store<TS>::ldc(b.U + v * g.fsc + col + idx));
     }
   }
 }
