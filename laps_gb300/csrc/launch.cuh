@@ -51,6 +51,18 @@ template <class K> inline void set_smem(K kernel, int bytes) {
   if (bytes > 40 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
+// persistent kernels: as many blocks as are resident at once on the device (at least one per SM)
+#ifndef LAPS_PIPE_B
+#define LAPS_PIPE_B 1
+#endif
+template <class K> inline int persistent_blocks(K kernel, int threads, int smem) {
+  int per_sm = 0, dev = 0, nsm = 0;
+  LAPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+  LAPS_CK(cudaGetDevice(&dev));
+  LAPS_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  return (per_sm > 0 ? per_sm : 1) * nsm;
+}
+
 
 template <class T>
 void launch_col_plain(cudaStream_t stream, const typename Store<T>::C* in, typename Store<T>::C* out, long long fs, int nf, int N,

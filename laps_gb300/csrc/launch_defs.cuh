@@ -82,9 +82,19 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
     /* two buffers each, so only a single-tile block may drop the second; 3-D: the two inputs  */                      \
     const int smB = (a.P.two_d && CL::NTILE == 1) ? CL::SMEM : 2 * CL::SMEM;                                            \
     if (!a.P.two_d && col_one_buffer<T, NN>()) throw Error{LAPS_EINVAL, "column tiles exceed shared memory"};             \
-    set_smem(k_passB<T, TS, NN>, smB);                                                                                  \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
+    /* FP32 lines up to 256 points: persistent blocks with two buffer sets (>= 3 blocks per SM) */                   \
+    if (LAPS_PIPE_B && !a.P.two_d && sizeof(typename Store<T>::C) == 8 && 4 * CL::SMEM <= 72 * 1024) {                \
+      const int smP = 4 * CL::SMEM;                                                                                     \
+      set_smem(k_passB_pipe<T, TS, NN>, smP);                                                                           \
+      const int nitems = grid.x * grid.y * grid.z;                                                                      \
+      const int pb = persistent_blocks(k_passB_pipe<T, TS, NN>, CL::THREADS, smP);                                      \
+      k_passB_pipe<T, TS, NN><<<nitems < pb ? nitems : pb, CL::THREADS, smP, stream>>>(B, a, kk, tw, *tm, nitems,      \
+                                                                                       grid.x, grid.y);                 \
+      break;                                                                                                            \
+    }                                                                                                                   \
+    set_smem(k_passB<T, TS, NN>, smB);                                                                                  \
     k_passB<T, TS, NN><<<grid, CL::THREADS, smB, stream>>>(B, a, kk, tw, *tm);                                          \
     break;                                                                                                              \
   }

@@ -238,6 +238,106 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS)
   for (int m = 0; m < CL::EPT; m++) Store<T>::stc(out + (long long)x.j(m) * g.kxp, Store<T>::ldc(x.at(0, m)));
 }
 
+// Pass B for FP32 lines of a 3-D run, persistent and double-buffered: each block takes items
+// (kx tile, z tile, output f) in turn, and the TMA loads of its next item go out before the
+// current item is combined, transformed and stored, so that the loads' latency overlaps the
+// block's own work instead of leaving it idle between one-shot launches.  Two buffer sets of
+// two buffers per tile (ColCtx with 4 buffers), one mbarrier per buffer, reused every other
+// item with its phase parity kept in a register.
+template <class T, class TS, int NY>
+__global__ void __launch_bounds__(Col<T, NY>::THREADS)
+    k_passB_pipe(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twy,
+                 const __grid_constant__ CUtensorMap tmap, int nitems, int nbx, int nby) {
+  const PT<T>& pc = kk.pc;
+  const KTab<T>& K = kk.K;
+  using CL = Col<T, NY>;
+  using C = typename Store<T>::C;
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  __shared__ __align__(8) uint64_t tbar[4];
+  if (a.st->halt) return;
+  ColCtx<T, NY, 4> x(reinterpret_cast<C*>(smem_tma));
+  const Geo& g = a.g;
+  const int vt = a.P.variant == LAPS_VARIANT_3DI ? 2 : 0;
+  const T rr = Real<T>::from_d(a.st->r_ratio);
+  // barrier 2 set + k holds buffer k of a set; bit i of ph is the parity barrier i waits on next
+  uint32_t ph = 0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 4; i++) mbar_init(&tbar[i], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto wait_buf = [&](int i) -> bool {  // every thread; false (after reporting) when the wait ran out
+    const bool good = mbar_wait(&tbar[i], (ph >> i) & 1u);
+    ph ^= 1u << i;
+    if (!good) atomicOr(&a.st->status, LAPS_STATUS_DEVICE_TIMEOUT);
+    return __syncthreads_and(good) != 0;
+  };
+  // the loads of item `it` into buffer set `set` (thread 0)
+  auto issue = [&](int set, int it) {
+    if (threadIdx.x != 0) return;
+    const int bx = it % nbx, by = (it / nbx) % nby, f = it / (nbx * nby);
+    const BTab e = c_btab[vt][f];
+    const int nin = e.in1 >= 0 ? 2 : 1;
+    constexpr int EW = (int)(sizeof(C) / 8);
+    const KeptCopies kc(g.ky_lo, g.ky_hi, NY, tile_gran((int)sizeof(C)));
+    const int nc = kc.count(NY);
+    const int z0 = by * CL::NTILE;
+    const int nt = g.nz - z0 < CL::NTILE ? g.nz - z0 : CL::NTILE;
+    for (int k = 0; k < nin; k++) {
+      uint64_t* bar = &tbar[set * 2 + k];
+      mbar_arrive_expect_tx(bar, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(C)));
+      for (int t = 0; t < nt; t++) {
+        C* dst = reinterpret_cast<C*>(smem_tma) + (t * 4 + set * 2 + k) * NY * TX;  // tile t, set, buffer k
+        for (int i = 0; i < nc; i++) {
+          const int y0 = kc.start(i, NY);
+          tma_load_3d(dst + y0 * TX, &tmap, bx * TX * EW, y0, (k == 0 ? e.in0 : e.in1) * g.nz + z0 + t, bar);
+        }
+      }
+    }
+  };
+  int it = blockIdx.x;
+  if (it >= nitems) return;
+  issue(0, it);
+#pragma unroll 1
+  for (int set = 0; it < nitems; it += gridDim.x, set ^= 1) {
+    const int nxt = it + gridDim.x;
+    if (nxt < nitems) {
+      // the other set was last read in the previous item, which ended on a block barrier
+      if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(set ^ 1, nxt);
+    }
+    const int bx = it % nbx, by = (it / nbx) % nby, f = it / (nbx * nby);
+    const BTab e = c_btab[vt][f];
+    const int nin = e.in1 >= 0 ? 2 : 1;
+    const int kx = bx * TX + x.c, z = by * CL::NTILE + x.tl;
+    const bool ok = kx < g.kx_keep && z < g.nz;
+    const long long col = (long long)z * g.ny * g.kxp + kx;
+    const bool kf = e.f0 > 1 || e.f0 < 0 || e.f1 > 1 || e.f1 < 0;
+    if (!wait_buf(set * 2) || (nin > 1 && !wait_buf(set * 2 + 1))) return;
+    C* b0 = x.buf(set * 2);
+#pragma unroll
+    for (int m = 0; m < CL::EPT; m++) {
+      const int ky = x.j(m);
+      cx<T> v = cx_zero<T>();
+      if (ok && g.ky_in(ky)) {
+        T ax = pc.zero, ay = pc.zero, az;
+        if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+        v = bterm(Store<T>::ldc(x.at(set * 2, m)), e.f0, ax, ay);
+        if (nin > 1) v = v + bterm(Store<T>::ldc(x.at(set * 2 + 1, m)), e.f1, ax, ay);
+      }
+      Store<T>::stc(x.at(set * 2, m), v);
+    }
+    __syncthreads();
+    fft_lines<T, NY, +1, TX, 1>(b0, x.c, x.t, true, twy, 1);
+    if (ok) {
+      C* out = b.W2 + f * g.fsc + col;
+#pragma unroll
+      for (int m = 0; m < CL::EPT; m++) Store<T>::stc(out + (long long)x.j(m) * g.kxp, Store<T>::ldc(x.at(set * 2, m)));
+    }
+    __syncthreads();
+  }
+}
+
 // ============================================================================ pass C
 // Per x-row (y, z): c2r of the inputs, the real-space physics, the CFL minimum of vardt when
 // asked, and r2c of the outputs.
