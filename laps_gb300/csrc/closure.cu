@@ -19,8 +19,9 @@
 // which serve the three dx taps.  Operand layout in shared memory (no swizzle, K-major): core
 // matrices of 8 rows x 16 bytes stored contiguously and one after the other along M, so every
 // row lies 16 bytes after the previous one and the operand of tap dx is the same stage with
-// its start moved by dx rows; chunk k of 8 channels is one TMA box of 130 rows (2080 B), so
-// core matrices adjacent in M are 128 B apart and those adjacent in K 2080 B apart.  The packed
+// its start moved by dx rows; chunk k of 8 channels is one TMA box of 130 rows (2080 B) at a
+// 2176-byte stride (TMA destinations sit on 128-byte boundaries), so core matrices adjacent in
+// M are 128 B apart and those adjacent in K 2176 B apart.  The packed
 // weights of a tap are [K chunk][N rows][8], N-adjacent 128 B apart, K-adjacent N * 16 B apart.
 //
 // Roles (192 threads, persistent over tiles): warp 0 issues the TMA loads, warp 1 allocates
@@ -135,8 +136,11 @@ __device__ __forceinline__ float gelu_grad(float z) {
 
 template <int KC, int NP> struct ConvCfg {
   static constexpr int A_ROWS = CONV_TILE + 2;                // x0 - 1 .. x0 + 128: the three dx taps
-  static constexpr int A_CHUNK = A_ROWS * 16;                 // 8 channels of those voxels
+  static constexpr int A_BOX = A_ROWS * 16;                   // 8 channels of those voxels (one TMA box)
+  // chunk stride: a TMA destination in shared memory must be 128-byte aligned
+  static constexpr int A_CHUNK = (A_BOX + 127) / 128 * 128;
   static constexpr int A_BYTES = KC * A_CHUNK;                // one (dz, dy) stage
+  static_assert(A_CHUNK % 128 == 0 && A_BYTES % 128 == 0, "TMA destinations on 128-byte boundaries");
   static constexpr int B_TAP = KC * NP * 16;                  // one tap of packed weights
   static constexpr int B_BYTES = 27 * B_TAP;
   // an operand read with its two strides exchanged would reach 16 x 2 KB past a stage's start:
@@ -209,7 +213,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
           const int dz = t / 3, dy = t % 3;
           const int zz = (z + dz - 1 + a.nz) % a.nz, yy = (y + dy - 1 + a.ny) % a.ny;
           const int row = (zz * a.ny + yy) * pitch + x0;
-          mbar_arrive_expect_tx(&full[s], CF::A_BYTES);
+          // (a destination off its 128-byte boundary is not loaded: the error word is set and
+          // the wait on this stage runs out instead of the copy faulting)
+          const bool aligned = (smem_u32(A + s * CF::A_BYTES) & 127u) == 0;
+          if (!aligned) {
+            atomicExch(a.err, 2);
+            bail = 1;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], KC * CF::A_BOX);
 #pragma unroll
           for (int k = 0; k < KC; k++) tma_load_2d(A + s * CF::A_BYTES + k * CF::A_CHUNK, &tx, k * 8, row, &full[s]);
           issued |= 1u << s;
