@@ -128,14 +128,15 @@ def main(argv=None):
     ap.add_argument("--train-seeds", default="10,11,12,13")
     ap.add_argument("--eval-seed", type=int, default=20)
     ap.add_argument("--warm", type=int, default=150)
-    ap.add_argument("--snaps", type=int, default=10)
-    ap.add_argument("--every", type=int, default=15)
-    ap.add_argument("--iters", type=int, default=600)
+    ap.add_argument("--snaps", type=int, default=20)
+    ap.add_argument("--every", type=int, default=8)
+    ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--eval-steps", type=int, default=150, help="fine steps of the evaluation interval")
     ap.add_argument("--threshold", type=float, default=0.05)
     args = ap.parse_args(argv)
-    prec_fine, prec_coarse = ffi.PREC_FP32_F64, ffi.PREC_FP64
+    # both grids in FP32 transforms with an FP64 state (RK accumulation, CFL, diagnostics)
+    prec_fine, prec_coarse = ffi.PREC_FP32_F64, ffi.PREC_FP32_F64
     n = args.fine // args.ratio
     t0 = time.perf_counter()
     states, targets = dataset(ffi, closure, [int(s) for s in args.train_seeds.split(",")], args.fine, args.ratio,
