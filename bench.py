@@ -331,7 +331,7 @@ def pinned_buffers(prim, local):
         return (np.ascontiguousarray(prim), np.empty((8,) + prim.shape[1:]), np.empty((4,) + prim.shape[1:]), False)
 
 
-def end_to_end(p, bufs, steps, npts, ws):
+def end_to_end(p, bufs, steps, npts, ws, sched=None):
     """The metric through the C-ABI with host buffers: upload of the primitive state from
     pinned host memory, `steps` laps_step(1) calls (each returns time, dt and status to the
     host), download of the final conserved state and primitives; host clock, max over ranks.
@@ -344,6 +344,8 @@ def end_to_end(p, bufs, steps, npts, ws):
     host_in, host_out, host_prim, pinned = bufs
     dptr = ctypes.POINTER(ctypes.c_double)
     ctx = ffi.Laps(p)
+    if sched is not None:
+        ctx.set_schedule(sched)
     ctx.upload_state(host_in, primitive=True)
     ctx.set_time(0.0)
     ctx.step(2)
@@ -526,12 +528,20 @@ def measure_mode(mode, p0, prim, args, npts, bufs, ws, local, with_clocks=False)
     state resident in HBM), the graph path, the end-to-end leg, and the roofline figures."""
     from laps_gb300 import ffi
 
+    from laps_gb300 import autotune
+
     q = ffi.laps_params.from_buffer_copy(p0)
     q.precision = PRECISIONS[mode][0]
     g = ffi.Laps(q)
     g.upload_state(prim, primitive=True)
     g.set_time(0.0)
     g.step(max(args.warmup, 3))
+    tuned = None
+    if not args.no_tune:  # the execution schedule (outside the timed region; cached on disk)
+        tuned = autotune.tune(g, steps=2)
+        g.upload_state(prim, primitive=True)  # the timed steps start from the same state
+        g.set_time(0.0)
+        g.step(max(args.warmup, 3))
     info = g.info()
     barrier(ws)
     clk = Clocks(local) if with_clocks else None
@@ -552,8 +562,11 @@ def measure_mode(mode, p0, prim, args, npts, bufs, ws, local, with_clocks=False)
            "dtype": PRECISIONS[mode][1], "graph_ms_per_step": graph_ms,
            "pass_ms_per_step": {PASS_NAMES[i]: pass_ms[i] / args.steps for i in range(6)},
            "roofline": roof, "passes_hbm": per_pass,
-           "e2e": end_to_end(q, bufs, args.steps, npts, ws),
+           "e2e": end_to_end(q, bufs, args.steps, npts, ws, None if args.no_tune else tuned["bits"]),
            "_info": info, "_pass_ms": pass_ms}
+    if tuned is not None:
+        res["schedule"] = {"bits": tuned["bits"], "from_cache": tuned["from_cache"],
+                           "candidates_ms_per_step": {str(b): round(t, 4) for b, t in tuned["times_ms"].items()}}
     if clk:
         res["clocks"] = clk.summary()
     if mode == "fp64" and not SHAPE and WL["variant"] == 0:
@@ -579,6 +592,19 @@ def run_ensemble(args):
     for i, prim in enumerate(prims):
         b.members[i].upload_state(prim, primitive=True)
         b.members[i].set_time(0.0)
+    schedules = {}
+    if not args.no_tune:  # one tuning per member kind (grid, precision, ...), then the cache
+        from laps_gb300 import autotune
+
+        cache = autotune.load_cache()
+        for i, prim in enumerate(prims):
+            m = b.members[i]
+            r = autotune.tune(m, steps=2, cache=cache)
+            schedules[r["key"]] = r["bits"]
+            if not r["from_cache"]:
+                m.upload_state(prim, primitive=True)
+                m.set_time(0.0)
+        autotune.save_cache(cache)
     b.step(max(args.warmup, 3))
     with Clocks(0) as clk:
         t0 = time.perf_counter()
@@ -608,6 +634,7 @@ def run_ensemble(args):
                    "timing": "host clock around laps_batch_step (one graph launch per step)",
                    "l2": "inputs larger than L2"},
         "status_nonzero_members": int((st != 0).sum()),
+        "schedules": schedules,
         "gpu_launches": None,
         "e2e": {"value": npts * args.steps / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -681,6 +708,8 @@ def run_ours(args):
         "e2e": head["e2e"],
         "clocks": head["clocks"],
     }
+    if "schedule" in head:
+        line["config"]["schedule"] = head["schedule"]
     if plain:
         line["plain"] = plain
         line["vs_plain"] = {k: head["value"] / v["value"] for k, v in plain.items()}
@@ -740,6 +769,8 @@ def main():
     ap.add_argument("--err-steps", type=int, default=500, dest="err_steps",
                     help="steps of the FP32-vs-FP64 error check of the fp32 modes (the workload's step count)")
     ap.add_argument("--no-cufft", action="store_true", dest="no_cufft", help="skip the cuFFT yardstick")
+    ap.add_argument("--no-tune", action="store_true", dest="no_tune",
+                    help="skip the schedule autotuner (laps_gb300/autotune.py) and run the default schedule")
     ap.add_argument("--no-closure", action="store_true", dest="no_closure",
                     help="skip the closure convolutions' tensor-core measurement")
     ap.add_argument("--cpu-steps", type=int, default=3, dest="cpu_steps",

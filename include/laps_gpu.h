@@ -376,6 +376,24 @@ int laps_closure_pack_input(const double* state, void* x, int n, double su, doub
 int laps_closure_unpack_output(const void* y, double* tau, int n, double s, void* stream);
 int laps_closure_forcing(const double* tau_spec, double* force_spec, int n, void* stream);
 
+/* Execution schedules.  No counterpart in the reference: choices of how the engine's kernels
+ * are launched that leave every result bit-identical, picked per grid, precision and device by
+ * the autotuner (laps_gb300/autotune.py, which times each with laps_step_profiled and caches
+ * the fastest).  Bits of laps_set_schedule (default 0):
+ *   LAPS_SCHED_PERSISTENT_B   pass B of FP32 lines up to 256 points (3-D) as persistent blocks
+ *                             with two buffer sets (the next tile's loads overlap this one's work)
+ *   LAPS_SCHED_NO_PREFETCH_E  pass E of FP32 lines without the L2 prefetch of the state and RK
+ *                             register rows it updates
+ *   LAPS_SCHED_INLINE_MASS    the continuity update in line before pass E instead of on a side
+ *                             stream beside pass D
+ * A change rebuilds the captured step graph (and an ensemble's, at its next step). */
+#define LAPS_SCHED_PERSISTENT_B 1
+#define LAPS_SCHED_NO_PREFETCH_E 2
+#define LAPS_SCHED_INLINE_MASS 4
+#define LAPS_SCHED_ALL 7
+int laps_set_schedule(laps_ctx* ctx, int bits);
+int laps_get_schedule(laps_ctx* ctx, int* bits);
+
 /* Bounded wait for all queued work of the context. */
 int laps_wait(laps_ctx* ctx, int timeout_ms);
 

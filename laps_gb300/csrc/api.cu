@@ -221,6 +221,11 @@ int laps_calc_rhs(laps_ctx* c, double* fnl) {
   return guarded(c, [&] { c->e->calc_rhs(fnl); });
 }
 int laps_dealias(laps_ctx* c) { return guarded(c, [&] { c->e->dealias_state(); }); }
+int laps_set_schedule(laps_ctx* c, int bits) { return guarded(c, [&] { c->e->set_schedule(bits); }); }
+int laps_get_schedule(laps_ctx* c, int* bits) {
+  if (!bits) return fail(c, LAPS_EINVAL, "null output pointer");
+  return guarded(c, [&] { *bits = c->e->schedule(); });
+}
 int laps_state_real_device(laps_ctx* c, double* uu_dev) {
   if (!uu_dev) return fail(c, LAPS_EINVAL, "null buffer");
   return guarded(c, [&] { c->e->state_real_device(uu_dev); });
@@ -258,6 +263,7 @@ struct laps_batch {
   std::vector<laps_ctx*> m;
   cudaStream_t origin = nullptr;
   cudaGraphExec_t graph = nullptr;
+  long long sched_changes = 0;  // members' schedule changes when the graph was captured
   cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
   std::vector<cudaEvent_t> ev_join;
   int dev = 0;
@@ -370,6 +376,13 @@ int laps_batch_step(laps_batch* b, int nsteps, double* time, double* dt, int* st
         LAPS_CK(cudaEventRecord(b->ev_join[i], b->m[i]->e->get_stream()));
         LAPS_CK(cudaStreamWaitEvent(b->origin, b->ev_join[i], 0));
       }
+      long long changes = 0;  // a member's schedule changed since the capture: capture again
+      for (int i = 0; i < n; i++) changes += b->m[i]->e->schedule_changes();
+      if (b->graph && changes != b->sched_changes) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+      }
+      b->sched_changes = changes;
       if (!b->graph) {
         cudaGraph_t gr;
         LAPS_CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));

@@ -110,6 +110,9 @@ class EngineBase {
   virtual const laps_params& params() const = 0;
   // device-side exchange with a caller (the closure): the 8 conserved real fields into a
   // device buffer; U += scale * duf (reference spectral layout, 8 fields) then the dealias
+  virtual void set_schedule(int bits) = 0;
+  virtual int schedule() const = 0;
+  virtual int schedule_changes() const = 0;
   virtual void state_real_device(double* dst) = 0;
   virtual void add_spectral_device(const double* duf, double scale) = 0;
   // granular, unfused path (bisection against the reference's subroutines)
@@ -142,6 +145,9 @@ template <class T, class TS = T> class Engine : public EngineBase {
   int dev = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph_steady = nullptr;
+  // execution schedule (LAPS_SCHED_* bits) and the number of times it changed (an ensemble
+  // recaptures its graph when a member's count moves)
+  int sched = 0, sched_changes = 0;
   long long bytes = 0;
   std::vector<void*> allocs;
   Bufs<T, TS> B{};
@@ -467,6 +473,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     a.e_first = 0;
     a.rhs_only = rhs_mode;
     a.mass_done = 0;
+    a.sched = sched;
     return a;
   }
   // the map whose box matches the kept-row copies the kernel makes for a.g
@@ -522,7 +529,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     if (!dealiased) ao.g = gfull;
     // the continuity update reads and writes only the state and RK register, which pass D
     // does not touch: it runs on a side stream beside pass D, joined before pass E
-    const bool fork = ao.mass_from_state && !ao.rhs_only && P.variant != LAPS_VARIANT_3DI;
+    const bool fork = ao.mass_from_state && !ao.rhs_only && P.variant != LAPS_VARIANT_3DI && !(sched & LAPS_SCHED_INLINE_MASS);
     if (fork) {
       side_ready();
       LAPS_CK(cudaEventRecord(ev_fork, stream));
@@ -897,6 +904,19 @@ template <class T, class TS = T> class Engine : public EngineBase {
     LAPS_CK(cudaGetLastError());
     return out;
   }
+  void set_schedule(int bits) override {
+    if (bits < 0 || bits > LAPS_SCHED_ALL) throw Error{LAPS_EINVAL, "unknown schedule bits"};
+    if (bits == sched) return;
+    wait(tmo());
+    sched = bits;
+    sched_changes++;
+    if (graph_steady) {  // the captured step holds the previous schedule
+      cudaGraphExecDestroy(graph_steady);
+      graph_steady = nullptr;
+    }
+  }
+  int schedule() const override { return sched; }
+  int schedule_changes() const override { return sched_changes; }
   void state_real_device(double* dst) override {
     const double* rs = stage_real_state();
     LAPS_CK(cudaMemcpyAsync(dst, rs, 8 * gfull.fsr * sizeof(double), cudaMemcpyDeviceToDevice, stream));

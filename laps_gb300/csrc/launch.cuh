@@ -51,13 +51,7 @@ template <class K> inline void set_smem(K kernel, int bytes) {
   if (bytes > 40 * 1024) LAPS_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
-// persistent kernels: as many blocks as are resident at once on the device (at least one per SM).
-// LAPS_PIPE_B selects the persistent, double-buffered pass B for FP32 lines; measured at 256^3
-// it is slower than the one-shot blocks (1.05 against 0.80 ms per step: three resident blocks of
-// 64 KB overlap less than five one-shot blocks of 32 KB), so it is off by default.
-#ifndef LAPS_PIPE_B
-#define LAPS_PIPE_B 0
-#endif
+// persistent kernels: as many blocks as are resident at once on the device (at least one per SM)
 template <class K> inline int persistent_blocks(K kernel, int threads, int smem) {
   int per_sm = 0, dev = 0, nsm = 0;
   LAPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));

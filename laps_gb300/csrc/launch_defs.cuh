@@ -85,7 +85,7 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \
     /* FP32 lines up to 256 points: persistent blocks with two buffer sets (>= 3 blocks per SM) */                   \
-    if (LAPS_PIPE_B && !a.P.two_d && sizeof(typename Store<T>::C) == 8 && 4 * CL::SMEM <= 72 * 1024) {                \
+    if ((a.sched & LAPS_SCHED_PERSISTENT_B) && !a.P.two_d && sizeof(typename Store<T>::C) == 8 && 4 * CL::SMEM <= 72 * 1024) { \
       const int smP = 4 * CL::SMEM;                                                                                     \
       set_smem(k_passB_pipe<T, TS, NN>, smP);                                                                           \
       const int nitems = grid.x * grid.y * grid.z;                                                                      \

@@ -24,6 +24,7 @@ struct PassArgs {
                    // of its own before the momentum is overwritten)
   int rhs_only;    // store the right-hand side (fnl) in R and leave the state (laps_calc_rhs)
   int mass_done;   // the continuity update (k_mass_rk) was launched already, beside pass D
+  int sched;       // execution schedule bits (LAPS_SCHED_*): results do not depend on them
   StepState* st;
 };
 
@@ -1201,7 +1202,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
       using CSP = typename Store<TS>::C;
       constexpr int EWU = (int)(sizeof(CSP) / 8);
       const KeptCopies kp(g.kz_lo, g.kz_hi, NZ, 1);
-      const int npf = sizeof(C) == 8 ? kp.count(NZ) : 0;
+      const int npf = sizeof(C) == 8 && !(a.sched & LAPS_SCHED_NO_PREFETCH_E) ? kp.count(NZ) : 0;
       for (int t = 0; t < nt; t++) {
         const int kyt = g.ky_of(r0 + t);
         for (int i = 0; i < npf; i++) {

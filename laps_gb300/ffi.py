@@ -28,6 +28,7 @@ LAPS_STATUS_DEVICE_TIMEOUT = 4
 VARIANT_3DC, VARIANT_3DI, VARIANT_2DC = 0, 1, 2
 PREC_FP64, PREC_DD, PREC_FP32, PREC_FP32_F64 = 0, 1, 2, 3
 LAYOUT_PRIMITIVE, LAYOUT_CONSERVED = 0, 1
+SCHED_PERSISTENT_B, SCHED_NO_PREFETCH_E, SCHED_INLINE_MASS, SCHED_ALL = 1, 2, 4, 7
 
 
 class laps_params(C.Structure):
@@ -145,6 +146,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         "laps_get_time": (C.c_int, [vp, dp, dp]),
         "laps_get_info": (C.c_int, [vp, P(laps_info)]),
         "laps_last_error": (C.c_char_p, [vp]),
+        "laps_set_schedule": (C.c_int, [vp, C.c_int]),
+        "laps_get_schedule": (C.c_int, [vp, P(C.c_int)]),
         "laps_batch_create": (C.c_int, [P(laps_params), C.c_int, P(vp)]),
         "laps_batch_size": (C.c_int, [vp]),
         "laps_batch_member": (C.c_int, [vp, C.c_int, P(vp)]),
@@ -328,6 +331,15 @@ class Laps:
         t, d = C.c_double(), C.c_double()
         self._ck(self.lib.laps_get_time(self.h, C.byref(t), C.byref(d)))
         return t.value, d.value
+
+    def set_schedule(self, bits: int):
+        """Execution schedule bits (SCHED_*): bit-identical results, different launch plans."""
+        self._ck(self.lib.laps_set_schedule(self.h, int(bits)))
+
+    def schedule(self) -> int:
+        v = C.c_int()
+        self._ck(self.lib.laps_get_schedule(self.h, C.byref(v)))
+        return v.value
 
     def info(self) -> laps_info:
         i = laps_info()
