@@ -23,7 +23,7 @@ beside the hand-written passes (outside the timed region).
 --impl reference: the reference's CPU algorithm on the machine's host cores - the C++/OpenMP
 restatement with its own FFT (oracle/laps3d_omp.cpp; the reference itself needs Fortran, MPI
 and FFTW, which the box does not have) - timed over the same --warmup / --steps of the same
-workload; `cpu_baseline` in our arm is the same code on a 1 + 3 step sample.
+workload; `cpu_baseline` in our arm is the same code on a 1 + 5 step sample.
 
 For N > 1 (torchrun) every rank advances its own independent replica ("replicas only":
 one run does not shard); value = all ranks' grid-point-steps / the slowest rank's time.
@@ -773,7 +773,7 @@ def main():
                     help="skip the schedule autotuner (laps_gb300/autotune.py) and run the default schedule")
     ap.add_argument("--no-closure", action="store_true", dest="no_closure",
                     help="skip the closure convolutions' tensor-core measurement")
-    ap.add_argument("--cpu-steps", type=int, default=3, dest="cpu_steps",
+    ap.add_argument("--cpu-steps", type=int, default=5, dest="cpu_steps",
                     help="timed steps of the CPU baseline (after one warm-up step)")
     ap.add_argument("--no-err", action="store_true", dest="no_err")
     ap.add_argument("--ref-steps", type=int, default=0, dest="ref_steps",
