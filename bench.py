@@ -624,6 +624,29 @@ def run_ensemble(args):
     sizes = {}
     for m in ms:
         sizes[m["n"]] = sizes.get(m["n"], 0) + 1
+    # CPU baseline: the 2-D numpy restatement on one member of each grid size, 1 warm-up + 2
+    # timed steps each (a bounded sample; the same metric over the sampled members)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import laps3d
+
+        pts, el, seen = 0, 0.0, set()
+        for m, prim in zip(ms, prims):
+            if m["n"] in seen:
+                continue
+            seen.add(m["n"])
+            kw = {k: v for k, v in m["kw"].items() if k not in ("variant", "nx", "ny", "nz")}
+            o = laps3d.restart2d(m["n"], kw, prim)
+            o.dt = 0.0
+            o.step()
+            t0 = time.perf_counter()
+            for _ in range(2):
+                o.step()
+            el += time.perf_counter() - t0
+            pts += 2 * m["n"] ** 2
+        cpu = {"value": pts / el, "unit": "grid-point-steps/s", "cores": laps3d._WORKERS, "kind": "port",
+               "sample": f"one member of each grid size {sorted(seen)}, 1 warm-up + 2 timed steps each "
+                         f"(numpy + scipy.fft 2-D restatement)"}
     line = {
         "metric": "grid-point-steps/s of a 64-member 2-D Hall-MHD ensemble", "value": value, "unit": "grid-point-steps/s",
         "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": el / args.steps * 1e3,
@@ -635,6 +658,7 @@ def run_ensemble(args):
                    "l2": "inputs larger than L2"},
         "status_nonzero_members": int((st != 0).sum()),
         "schedules": schedules,
+        "cpu_baseline": cpu,
         "gpu_launches": None,
         "e2e": {"value": npts * args.steps / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
