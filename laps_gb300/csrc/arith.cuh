@@ -54,7 +54,10 @@ __device__ __forceinline__ dd dd_mul_f(dd a, float b) {
   return dd_fast_two_sum(p, e);
 }
 // exact scaling by a power of two
-__device__ __forceinline__ dd dd_ldexp(dd a, int e) { return {ldexpf(a.hi, e), ldexpf(a.lo, e)}; }
+__device__ __forceinline__ dd dd_ldexp(dd a, int e) {  // -127 < e < 128 (the transforms' normalisations)
+  const float s = __int_as_float((127 + e) << 23);
+  return {a.hi * s, a.lo * s};
+}
 __device__ __forceinline__ dd operator/(dd a, dd b) {
   float q1 = __fdiv_rn(a.hi, b.hi);
   dd r = a - dd_mul_f(b, q1);
@@ -97,7 +100,11 @@ template <> struct Real<double> {
   __device__ __forceinline__ static double sqrt_(double x) { return sqrt(x); }
   __device__ __forceinline__ static double abs_(double x) { return fabs(x); }
   __device__ __forceinline__ static double max_(double a, double b) { return (a > b || a != a) ? a : b; }
-  __device__ __forceinline__ static double mul_pow2(double a, int e) { return ldexp(a, e); }
+  // a * 2^e for the transforms' normalisations (-1022 < e < 1024): one multiplication by the
+  // exact power of two built from its exponent field
+  __device__ __forceinline__ static double mul_pow2(double a, int e) {
+    return a * __longlong_as_double((long long)(1023 + e) << 52);
+  }
   __device__ __forceinline__ static float lead(double x) { return (float)x; }
   __device__ __forceinline__ static bool isnan_(double x) { return x != x; }
   __device__ __forceinline__ static double min_(double a, double b) { return b < a ? b : a; }
