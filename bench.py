@@ -630,7 +630,7 @@ def run_ensemble(args):
     if not args.no_cpu:
         from oracle import laps3d
 
-        pts, el, seen = 0, 0.0, set()
+        pts, cpu_s, seen = 0, 0.0, set()
         for m, prim in zip(ms, prims):
             if m["n"] in seen:
                 continue
@@ -642,9 +642,9 @@ def run_ensemble(args):
             t0 = time.perf_counter()
             for _ in range(2):
                 o.step()
-            el += time.perf_counter() - t0
+            cpu_s += time.perf_counter() - t0
             pts += 2 * m["n"] ** 2
-        cpu = {"value": pts / el, "unit": "grid-point-steps/s", "cores": laps3d._WORKERS, "kind": "port",
+        cpu = {"value": pts / cpu_s, "unit": "grid-point-steps/s", "cores": laps3d._WORKERS, "kind": "port",
                "sample": f"one member of each grid size {sorted(seen)}, 1 warm-up + 2 timed steps each "
                          f"(numpy + scipy.fft 2-D restatement)"}
     line = {
