@@ -172,6 +172,101 @@ template <class T> __device__ __forceinline__ cx<T> times_i(cx<T> a) { return {-
 template <class T> __device__ __forceinline__ cx<T> times_mi(cx<T> a) { return {a.im, -a.re}; }
 template <class T> __device__ __forceinline__ cx<T> cx_zero() { return {Real<T>::cst(0.0), Real<T>::cst(0.0)}; }
 
+// ------------------------------------------------------- packed float-float complex values
+// Blackwell issues an FP32 add, multiply or fused multiply-add on the two lanes of a 64-bit
+// register pair as one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn, sub.rn.f32x2).  A
+// complex float-float value maps onto them with its real part in lane x and its imaginary part
+// in lane y: h = (re.hi, im.hi), l = (re.lo, im.lo).  Each lane runs the scalar algorithm above
+// step for step with the same round-to-nearest operations, so every result is bit-identical to
+// the scalar form, in half the arithmetic instructions.
+#ifndef LAPS_PACKED_DD
+#define LAPS_PACKED_DD 1
+#endif
+struct pdd {
+  float2 h, l;
+};
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ pdd pk(cx<dd> a) { return {make_float2(a.re.hi, a.im.hi), make_float2(a.re.lo, a.im.lo)}; }
+__device__ __forceinline__ cx<dd> upk(pdd a) { return {{a.h.x, a.l.x}, {a.h.y, a.l.y}}; }
+__device__ __forceinline__ pdd pbcast(dd s) { return {make_float2(s.hi, s.hi), make_float2(s.lo, s.lo)}; }
+// dd_two_sum / dd_fast_two_sum per lane: s in .h, error in .l
+__device__ __forceinline__ pdd p_two_sum(float2 a, float2 b) {
+  const float2 s = f2add(a, b);
+  const float2 bb = f2sub(s, a);
+  return {s, f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb))};
+}
+__device__ __forceinline__ pdd p_fast_two_sum(float2 a, float2 b) {
+  const float2 s = f2add(a, b);
+  return {s, f2sub(b, f2sub(s, a))};
+}
+// a + b and a - b per lane (operator+ of dd; a - b as a + (-b), whose roundings are those of
+// the subtractions written here: RN(-x - y) = -RN(x + y))
+__device__ __forceinline__ pdd padd(pdd a, pdd b) {
+  const pdd s = p_two_sum(a.h, b.h);
+  return p_fast_two_sum(s.h, f2add(s.l, f2add(a.l, b.l)));
+}
+__device__ __forceinline__ pdd psub(pdd a, pdd b) {
+  const float2 s = f2sub(a.h, b.h);
+  const float2 bb = f2sub(s, a.h);
+  const float2 e = f2sub(f2sub(a.h, f2sub(s, bb)), f2add(b.h, bb));
+  return p_fast_two_sum(s, f2add(e, f2sub(a.l, b.l)));
+}
+// a * m per lane (operator* of dd), m one multiplier per lane
+__device__ __forceinline__ pdd pmul(pdd a, pdd m) {
+  const float2 p = f2mul(a.h, m.h);
+  float2 e = f2fma(a.h, m.h, f2neg(p));
+  e = f2fma(a.h, m.l, e);
+  e = f2fma(a.l, m.h, e);
+  return p_fast_two_sum(p, e);
+}
+
+// FP32 complex sums and differences as one two-lane instruction each
+#ifndef LAPS_PACKED_F32
+#define LAPS_PACKED_F32 1
+#endif
+#if LAPS_PACKED_F32
+__device__ __forceinline__ cx<float> operator+(cx<float> a, cx<float> b) {
+  const float2 r = f2add(make_float2(a.re, a.im), make_float2(b.re, b.im));
+  return {r.x, r.y};
+}
+__device__ __forceinline__ cx<float> operator-(cx<float> a, cx<float> b) {
+  const float2 r = f2sub(make_float2(a.re, a.im), make_float2(b.re, b.im));
+  return {r.x, r.y};
+}
+#endif
+
+#if LAPS_PACKED_DD
+__device__ __forceinline__ cx<dd> operator+(cx<dd> a, cx<dd> b) { return upk(padd(pk(a), pk(b))); }
+__device__ __forceinline__ cx<dd> operator-(cx<dd> a, cx<dd> b) { return upk(psub(pk(a), pk(b))); }
+__device__ __forceinline__ cx<dd> operator*(cx<dd> a, dd s) { return upk(pmul(pk(a), pbcast(s))); }
+// The complex product below, lane x the real part and lane y the imaginary part of each step.
+__device__ __forceinline__ cx<dd> operator*(cx<dd> a, cx<dd> b) {
+  const float2 arh = make_float2(a.re.hi, a.re.hi), arl = make_float2(a.re.lo, a.re.lo);
+  const float2 aih = make_float2(-a.im.hi, a.im.hi), ail = make_float2(-a.im.lo, a.im.lo);
+  const float2 bh = make_float2(b.re.hi, b.im.hi), bl = make_float2(b.re.lo, b.im.lo);
+  const float2 bhs = make_float2(b.im.hi, b.re.hi), bls = make_float2(b.im.lo, b.re.lo);
+  const float2 p = f2mul(arh, bh), q = f2mul(aih, bhs);  // (p1, q1), (-p2, q2)
+  const float2 e1 = f2fma(arh, bh, f2neg(p)), e2 = f2fma(aih, bhs, f2neg(q));
+  const pdd s = p_two_sum(p, q);
+  float2 e = f2add(s.l, f2add(e1, e2));
+  e = f2fma(arh, bl, e);
+  e = f2fma(arl, bh, e);
+  e = f2fma(aih, bls, e);
+  e = f2fma(ail, bhs, e);
+  return upk(p_fast_two_sum(s.h, e));
+}
+#else
 // Complex float-float product with shared error terms (~36 FP32 instructions instead of 50).
 __device__ __forceinline__ cx<dd> operator*(cx<dd> a, cx<dd> b) {
   // re = a.re*b.re - a.im*b.im ; im = a.re*b.im + a.im*b.re
@@ -195,6 +290,7 @@ __device__ __forceinline__ cx<dd> operator*(cx<dd> a, cx<dd> b) {
   dd im = dd_fast_two_sum(t.hi, f);
   return {re, im};
 }
+#endif
 
 // ------------------------------------------------------------------------------ storage
 // How a value of type T lives in memory.  Complex values are one 16-byte (FP64, dd) or

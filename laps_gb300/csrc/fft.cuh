@@ -12,6 +12,8 @@
 // tiles use JS = TX, LS = 1 (a quarter-warp touches one 128-byte row: conflict-free);
 // rows use JS = 1, LS = line pitch.
 #pragma once
+#include <type_traits>
+
 #include "arith.cuh"
 
 namespace laps {
@@ -34,18 +36,29 @@ LAPS_KC(K_S8, 0.38268343236508977173);    // sin(pi/8)
 // x * exp(DIR * i * theta) for theta = pi/4 (w8), given cos = sin = sqrt(2)/2
 template <class T, int DIR> __device__ __forceinline__ cx<T> rot45(cx<T> x) {
   const T c = kc<T>(K_SQH_d, K_SQH_h, K_SQH_l);
+#if LAPS_PACKED_DD
+  // float-float: both components in one packed pass, (x -/+ i x) c, with the operations of
+  // the scalar form in each lane
+  if constexpr (std::is_same<T, dd>::value) return (x + (DIR < 0 ? times_mi(x) : times_i(x))) * c;
+#endif
   // DIR=-1: (1 - i)/sqrt2 * (a + ib) = ((a + b) + i (b - a)) / sqrt2
   if (DIR < 0) return {(x.re + x.im) * c, (x.im - x.re) * c};
   return {(x.re - x.im) * c, (x.im + x.re) * c};
 }
 template <class T, int DIR> __device__ __forceinline__ cx<T> rot135(cx<T> x) {
   const T c = kc<T>(K_SQH_d, K_SQH_h, K_SQH_l);
+#if LAPS_PACKED_DD
+  if constexpr (std::is_same<T, dd>::value) return DIR < 0 ? times_mi(rot45<T, DIR>(x)) : times_i(rot45<T, DIR>(x));
+#endif
   // DIR=-1: (-1 - i)/sqrt2 * (a + ib) = ((b - a) + i (-a - b)) / sqrt2
   if (DIR < 0) return {(x.im - x.re) * c, -((x.re + x.im) * c)};
   return {-((x.re + x.im) * c), (x.re - x.im) * c};
 }
 // x * (c + DIR*i*s) with constants c, s
 template <class T, int DIR> __device__ __forceinline__ cx<T> rotcs(cx<T> x, T c, T s) {
+#if LAPS_PACKED_DD
+  if constexpr (std::is_same<T, dd>::value) return x * c + (DIR < 0 ? times_mi(x) : times_i(x)) * s;
+#endif
   if (DIR < 0) return {x.re * c + x.im * s, x.im * c - x.re * s};
   return {x.re * c - x.im * s, x.im * c + x.re * s};
 }
