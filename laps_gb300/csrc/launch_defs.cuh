@@ -65,8 +65,8 @@ void launch_rows_c2r(cudaStream_t stream, int nx, const typename Store<T>::C* in
 #define LAPS_CASE(NN)                                                                                                   \
   case NN: {                                                                                                            \
     using CL = Col<T, NN>;                                                                                              \
-    /* transform tiles, then the state tiles they are formed from */                                                 \
-    const int sm = CL::SMEM + CL::NTILE * NN * TX * (int)sizeof(typename Store<TS>::C);                                 \
+    /* the state tiles, which the transform tiles overwrite once every thread has read its elements */             \
+    const int sm = CL::NTILE * NN * TX * (int)sizeof(typename Store<TS>::C);                                            \
     set_smem(k_passA<T, TS, NN>, sm);                                                                                   \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nky() + CL::NTILE - 1) / CL::NTILE,                                     \
               a.P.variant == LAPS_VARIANT_3DI ? 12 : (a.hall ? 10 : 8));                                                \

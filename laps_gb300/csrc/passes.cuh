@@ -69,8 +69,11 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
   __shared__ __align__(8) uint64_t tbar[2];
   if (a.st->halt) return;
   ColCtx<T, NZ, 1> x(reinterpret_cast<C*>(smem_tma));
-  // the state tiles (whole z columns, state type) after the NTILE transform tiles
-  CS* raw = reinterpret_cast<CS*>(smem_tma + CL::NTILE * NZ * TX * (int)sizeof(C)) + x.tl * NZ * TX;
+  // the state tiles (whole z columns, state type) share the block's shared memory with the
+  // transform tiles: every thread takes its elements from them into registers before the
+  // first transform element is written (the state type is at least as wide as the compute type)
+  static_assert(sizeof(CS) >= sizeof(C), "state tiles cover the transform tiles");
+  CS* raw = reinterpret_cast<CS*>(smem_tma) + x.tl * NZ * TX;
   const Geo& g = a.g;
   const int f = blockIdx.z;
   const ATab e = c_atab[a.P.variant == LAPS_VARIANT_3DI ? 1 : 0][f];
@@ -92,7 +95,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
       const int nt = g.nky() - r0 < CL::NTILE ? g.nky() - r0 : CL::NTILE;
       tl.expect(0, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(CS)));
       for (int t = 0; t < nt; t++) {
-        CS* dst = reinterpret_cast<CS*>(smem_tma + CL::NTILE * NZ * TX * (int)sizeof(C)) + t * NZ * TX;
+        CS* dst = reinterpret_cast<CS*>(smem_tma) + t * NZ * TX;
         for (int i = 0; i < nc; i++) {
           const int z0 = kc.start(i, NZ);
           tl.copy(0, dst + z0 * TX, &tmap, blockIdx.x * TX * EW, g.ky_of(r0 + t), e.src * g.nz + z0);
@@ -101,19 +104,24 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
     }
     if (!tl.wait(0, a.st)) return;
   }
+  cx<T> v[CL::EPT];
 #pragma unroll
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
-    cx<T> v = cx_zero<T>();
+    v[m] = cx_zero<T>();
     if (ok && g.kz_in(kz)) {
       // (FP32 lines of an FP64 state: the conversion on the integer pipes)
-      if constexpr (std::is_same<T, float>::value) v = IncCvt<TS>::to_f32(Store<TS>::ldc(raw + kz * TX + x.c));
-      else v = cvtc<T>(Store<TS>::ldc(raw + kz * TX + x.c));
-      if (e.mult < 0) v = -mul_i(v, K.kzd[kz]);
-      else if (e.mult > 0) v = mul_i(v, K.kzd[kz]);
+      if constexpr (std::is_same<T, float>::value) v[m] = IncCvt<TS>::to_f32(Store<TS>::ldc(raw + kz * TX + x.c));
+      else v[m] = cvtc<T>(Store<TS>::ldc(raw + kz * TX + x.c));
+      if (e.mult < 0) v[m] = -mul_i(v[m], K.kzd[kz]);
+      else if (e.mult > 0) v[m] = mul_i(v[m], K.kzd[kz]);
     }
-    Store<T>::stc(x.at(0, m), v);
   }
+  // same element sizes: each thread rewrites only the slots it has read; narrower transform
+  // elements overwrite other threads' state elements, so all reads come first
+  if constexpr (sizeof(CS) != sizeof(C)) __syncthreads();
+#pragma unroll
+  for (int m = 0; m < CL::EPT; m++) Store<T>::stc(x.at(0, m), v[m]);
   __syncthreads();
   fft_lines<T, NZ, +1, TX, 1>(x.buf(0), x.c, x.t, true, twz, 1);
   if (!ok) return;
