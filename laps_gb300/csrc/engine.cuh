@@ -14,6 +14,27 @@ constexpr int TX = 8;  // columns per tile: 8 x 16 B = one 128-byte row
 // kxp = round_up(nx/2+1, 8), i.e. the reference's uu_fourier(kx,ky,kz,ivar) order
 // (src_compressible/mhdinit.f90:155-169) with padded rows.  Real arrays: (x, y, z, field)
 // exactly as the reference's uu(ix,iy,iz,ivar).
+// q = n / d for 0 <= n < 2^31 by one multiply-high, an add and a shift (Granlund & Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(n, m) + n) >> l; the sum stays below 2^32
+// for n < 2^31.  The magic numbers come from the host; on this GPU a runtime integer division
+// costs conversion instructions, which run on the slow FP64 pipe.
+struct FastDiv {
+  unsigned d, m, l;
+  FastDiv() = default;
+  explicit FastDiv(unsigned div) : d(div), m(0), l(0) {
+    while ((1ull << l) < div) l++;
+    m = (unsigned)((((1ull << 32) * ((1ull << l) - div)) / div) + 1);
+  }
+  __host__ __device__ __forceinline__ unsigned div(unsigned n) const {
+#ifdef __CUDA_ARCH__
+    return (__umulhi(n, m) + n) >> l;
+#else
+    return (unsigned)((((unsigned long long)n * m >> 32) + n) >> l);
+#endif
+  }
+};
+
 struct Geo {
   int nx, ny, nz, nh;     // nh = nx/2 + 1
   int kxp;                // spectral row pitch
@@ -74,7 +95,29 @@ struct StepState {
   int halt;                        // skip the rest of the step (dt floor)
   int ksq_plain;                   // k^2 still the grid_initialize sum (no R factor)
   unsigned int cfl32_bits;         // running min of the FP32 screen of the CFL step (bits of a float)
+  // the nearest floats of cc, ddc, ts, inv_tau and r_ratio for the FP32-increment updates,
+  // written with them (step_state_f32): a conversion from binary64 (and a binary64 division)
+  // issues at the FP64 pipe's rate on this GPU, too slow to repeat in every thread
+  float f_cc[3], f_ddc[3], f_ts[3], f_inv_tau, f_r_ratio;
+  double inv_rho0;  // 1 / rho0, with its nearest float
+  float f_inv_rho0;
+  double R0;        // radius0 (constant), and radius / radius0 with its nearest float (CFL)
+  double rfac;
+  float f_rfac;
 };
+__host__ __device__ inline void step_state_f32(StepState& s) {
+  for (int i = 0; i < 3; i++) {
+    s.f_cc[i] = (float)s.cc[i];
+    s.f_ddc[i] = (float)s.ddc[i];
+    s.f_ts[i] = (float)s.ts[i];
+  }
+  s.f_inv_tau = (float)s.inv_tau;
+  s.f_r_ratio = (float)s.r_ratio;
+  s.inv_rho0 = 1.0 / s.rho0;
+  s.f_inv_rho0 = (float)s.inv_rho0;
+  s.rfac = s.radius / s.R0;
+  s.f_rfac = (float)s.rfac;
+}
 
 // wave-number tables (element type T), rebuilt by a small kernel whenever R changes
 template <class T> struct KTab {

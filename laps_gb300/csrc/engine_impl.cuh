@@ -383,6 +383,8 @@ template <class T, class TS = T> class Engine : public EngineBase {
     s0.ksq_plain = 1;  // grid_initialize's k^2 until the first evolve_radius
     s0.rho0 = q.rho0 > 0 ? q.rho0 : 1.0;
     s0.istep = 0;
+    s0.R0 = P.R0;
+    step_state_f32(s0);
     LAPS_CK(cudaMemcpy(st, &s0, sizeof(s0), cudaMemcpyHostToDevice));
     npart = 4096;
     d_part = dalloc<double>((size_t)npart * 32);
@@ -829,6 +831,7 @@ template <class T, class TS = T> class Engine : public EngineBase {
     s.inv_tau = P.Ur != 0.0 ? 1.0 / (s.radius / P.Ur) : 0.0;
     s.r_ratio = p.radius0 / s.radius;
     s.ksq_plain = 0;
+    step_state_f32(s);
     LAPS_CK(cudaMemcpyAsync(st, &s, sizeof(s), cudaMemcpyHostToDevice, stream));
     tables();
     wait(tmo());

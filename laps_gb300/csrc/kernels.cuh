@@ -458,6 +458,7 @@ static __global__ void k_finalize_dt(StepState* st, double cfl, int dstep, int l
   st->ts[0] = 8.0 / 15.0 * dt;
   st->ts[1] = 2.0 / 15.0 * dt;
   st->ts[2] = 1.0 / 3.0 * dt;
+  step_state_f32(*st);
   if (dt < 0.00000001) {
     st->status |= LAPS_STATUS_DT_FLOOR;
     st->halt = 1;
@@ -479,6 +480,7 @@ static __global__ void k_advance_time(StepState* st, double R0, double Ur, int i
   st->inv_tau = Ur != 0.0 ? 1.0 / (st->radius / Ur) : 0.0;
   st->r_ratio = R0 / st->radius;
   st->ksq_plain = 0;
+  step_state_f32(*st);
 }
 
 }  // namespace laps

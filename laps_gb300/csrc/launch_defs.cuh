@@ -119,9 +119,16 @@ LAPS_COL_PASS(launch_passD, k_passD, nz)
     PassArgs a0 = a;                                                                                                    \
     a0.e_first = 0;                                                                                                     \
     if (a.mass_from_state) { /* continuity from the momentum first, then variables 1..7 */                             \
-      if (!a.mass_done) k_mass_rk<T, TS><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk);                             \
+      if (!a.mass_done) launch_mass_rk<T, TS>(stream, B, a, kk);                                                        \
       a0.e_first = 1;                                                                                                   \
       grid.z = 7;                                                                                                       \
+    }                                                                                                                   \
+    if constexpr (NN == 1) { /* 2-D: the elementwise form */                                                          \
+      const long long tot = (long long)a.g.kx_keep * a.g.nky();                                                        \
+      const long long nb = (tot + 255) / 256;                                                                           \
+      k_passE2d<T, TS><<<dim3((unsigned)(nb < 1216 ? nb : 1216), grid.z), 256, 0, stream>>>(B, a0, kk,                   \
+                                                                                               FastDiv(a.g.kx_keep));  \
+      break;                                                                                                            \
     }                                                                                                                   \
     k_passE<T, TS, NN><<<grid, CL::THREADS, 2 * CL::SMEM, stream>>>(B, a0, kk, tw, tm[0], tm[1], tm[2]);                                     \
     break;                                                                                                              \
@@ -160,7 +167,10 @@ void launch_passC_v(cudaStream_t stream, int N, Bufs<T, TS> B, PassArgs a, PassK
 // the continuity update alone (forked beside pass D by the step)
 template <class T, class TS>
 void launch_mass_rk(cudaStream_t stream, Bufs<T, TS> B, PassArgs a, PassK<T, TS> kk) {
-  k_mass_rk<T, TS><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk);
+  const long long tot = (long long)a.g.kx_keep * a.g.nky() * a.g.nkz();
+  const FastDiv dkx(a.g.kx_keep), dky(a.g.nky());
+  if (tot < (1ll << 31)) k_mass_rk<T, TS, unsigned><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk, dkx, dky);
+  else k_mass_rk<T, TS, long long><<<mass_rk_blocks(a.g), 256, 0, stream>>>(B, a, kk, dkx, dky);
   LAPS_CK(cudaGetLastError());
 }
 

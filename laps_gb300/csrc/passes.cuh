@@ -574,11 +574,21 @@ constexpr unsigned c_fused = 0x7FFFFu & ~((1u << 6) | (1u << 9) | (1u << 10));
 // Rows per block and lines per FFT batch: 24 lines of 2 rows hold the 22 inputs of two rows
 // (Hall) in one batch; when two rows of 19 line slots do not fit in shared memory (1024-point
 // rows of 16-byte elements) a block takes one row and batches of 12 lines.
-// Lines per batch of the 512- and 1024-point rows: 16 (256 / 512 threads) leaves 128 or more
-// registers per thread (24 spilled: 3-D incompressible 512^3 pass C 22.7 -> 18.3 ms per step);
+// Lines per batch of the 512-point rows: 16 (256 threads) leaves 128 or more registers per
+// thread (24 spilled: 3-D incompressible 512^3 pass C 22.7 -> 18.3 ms per step);
 // LAPS_PASSC_LB_LONG overrides it at build time for tuning sweeps.
 #ifndef LAPS_PASSC_LB_LONG
 #define LAPS_PASSC_LB_LONG 16
+#endif
+// 1024-point rows of FP32 lines: one half-length complex line per row (a warp per line, no
+// block barriers inside a transform) in batches of 32 lines (1024 threads): the 2-D ensemble's
+// 1024^2 members, pass C -4 % against paired rows in batches of 16 (LAPS_PASSC_PAIR_1024,
+// LAPS_PASSC_LB_1024 override it at build time)
+#ifndef LAPS_PASSC_LB_1024
+#define LAPS_PASSC_LB_1024 32
+#endif
+#ifndef LAPS_PASSC_PAIR_1024
+#define LAPS_PASSC_PAIR_1024 0
 #endif
 template <int NX, int CB> struct PassCCfg {
   static constexpr int H = NX / 2;
@@ -587,15 +597,15 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int NF = 19;             // line slots per row
   static constexpr int LC = RowLen<H>::V;   // padded complex per line
   static constexpr bool ONE_ROW = 2 * MUL * NF * LC * CB > 200 * 1024;
-  static constexpr int LB = ONE_ROW ? 12 : (NX >= 512 ? LAPS_PASSC_LB_LONG : 24 * MUL);  // lines per batch
+  static constexpr int LB = ONE_ROW ? 12 : (NX >= 1024 ? LAPS_PASSC_LB_1024 : NX >= 512 ? LAPS_PASSC_LB_LONG : 24 * MUL);  // lines per batch
   static constexpr int THREADS = LB * TPL;
   static constexpr int ROWS = ONE_ROW ? 1 : 2 * MUL;
   // Paired rows: rows 2p and 2p+1 of a field share one complex line of NX points,
   // z = x_2p + i x_2p+1, so a row pair takes one full-length complex FFT and no twiddled
-  // packing; 1024-point lines (two warps) pair too, with block barriers, while one-row blocks
-  // (1024-point rows of 16-byte types) keep the half-length form.
+  // packing (up to 512 points; 1024-point lines would take two warps and block barriers, so
+  // 1024-point rows keep the half-length form unless LAPS_PASSC_PAIR_1024 is set).
   static constexpr int TPLP = Plan<NX>::TPL;
-  static constexpr bool PAIRED = !ONE_ROW && TPLP <= 64;
+  static constexpr bool PAIRED = !ONE_ROW && TPLP <= 64 && (NX != 1024 || LAPS_PASSC_PAIR_1024);
   static constexpr bool LWARP = TPLP <= 32;  // a paired line within one warp (else two: block barriers)
   static constexpr int LCP = RowLen<NX>::V;   // padded complex per paired line
   static constexpr int LBP = THREADS / TPLP;  // paired lines per batch
@@ -692,7 +702,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   __shared__ int ncand, skip_ts;
   bool cand_late = false;  // block-uniform: the list waits for warp 0 at the end
   using PHS = typename std::conditional<INCOMP, FluxI<TS>, Flux<TS>>::type;
-  const TS rfac = Real<TS>::from_d(a.st->radius / a.P.R0);
+  const TS rfac = Real<TS>::from_d(a.st->rfac);  // radius / R0
   auto report = [&](TS tmin, bool nan_seen) {  // warp min, then one atomic per warp
     double dmin = Real<TS>::to_d(tmin);
     for (int o = 16; o > 0; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
@@ -721,7 +731,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     using PHF = typename std::conditional<INCOMP, FluxI<float>, Flux<float>>::type;
     __shared__ float red32[32];
     const PT<float> pf = pt_float(pc);
-    const float rfac_f = (float)(a.st->radius / a.P.R0);
+    const float rfac_f = a.st->f_rfac;
     constexpr int PPT = (CF::ROWS * NX + CF::THREADS - 1) / CF::THREADS;  // points per thread
     float d32[PPT];
     float m32 = __int_as_float(0x7f800000);
@@ -800,7 +810,9 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   }
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
   const T inv_tau = Real<T>::from_d(a.st->inv_tau);
-  const T inv_rho0 = Real<T>::from_d(1.0 / a.st->rho0);
+  T inv_rho0;
+  if constexpr (std::is_same<T, float>::value) inv_rho0 = a.st->f_inv_rho0;
+  else inv_rho0 = Real<T>::from_d(a.st->inv_rho0);
 #pragma unroll 1
   for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
     SR* base = point_base(p);
@@ -1143,11 +1155,19 @@ __device__ __forceinline__ RkCtx<T, TR> rk_ctx(const PassArgs& a, const PT<T>& p
   r.g = &a.g; r.P = &a.P; r.pc = &pc; r.K = &K;
   r.stage = a.stage;
   r.store_rk = a.store_rk;
-  r.cc = Real<T>::from_d(a.st->cc[a.stage]);
-  r.ddc = Real<T>::from_d(a.st->ddc[a.stage]);
-  r.ts = Real<T>::from_d(a.st->ts[a.stage]);
-  r.inv_tau = Real<T>::from_d(a.st->inv_tau);
-  r.rr = Real<T>::from_d(a.st->r_ratio);
+  if constexpr (std::is_same<T, float>::value) {  // the step state's FP32 copies
+    r.cc = a.st->f_cc[a.stage];
+    r.ddc = a.st->f_ddc[a.stage];
+    r.ts = a.st->f_ts[a.stage];
+    r.inv_tau = a.st->f_inv_tau;
+    r.rr = a.st->f_r_ratio;
+  } else {
+    r.cc = Real<T>::from_d(a.st->cc[a.stage]);
+    r.ddc = Real<T>::from_d(a.st->ddc[a.stage]);
+    r.ts = Real<T>::from_d(a.st->ts[a.stage]);
+    r.inv_tau = Real<T>::from_d(a.st->inv_tau);
+    r.rr = Real<T>::from_d(a.st->r_ratio);
+  }
   r.plain = a.st->ksq_plain;
   r.rhs_only = a.rhs_only;
   return r;
@@ -1246,8 +1266,8 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
   // FP32 tables
   constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
   const RkCtx<T, T> rkf = rk_ctx<T>(a, kk.pc, kk.K);
-  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
-  const float tsf = (float)a.st->ts[a.stage];
+  const float ccf = a.st->f_cc[a.stage], ddcf = a.st->f_ddc[a.stage], itf = a.st->f_inv_tau;
+  const float tsf = a.st->f_ts[a.stage];
   const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
   CS* U = b.U + v * g.fsc + col;
   C* R = b.R + v * g.fsc + col;
@@ -1293,24 +1313,76 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
   }
 }
 
+// Pass E of a 2-D run (nz = 1: the z transform is the identity): the same per-element tail
+// and time advance as k_passE, over the kept (kx, ky) elements of variable
+// v = blockIdx.y + e_first, read straight from W2 (k_passE's column tiles would hold one
+// element per thread here); a flat 32-bit index over the kept elements, split by FastDiv.
+template <class T, class TS>
+__global__ void __launch_bounds__(256) k_passE2d(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, FastDiv dkx) {
+  if (a.st->halt) return;
+  using CS = typename Store<TS>::C;
+  using C = typename Store<T>::C;
+  const Geo& g = a.g;
+  const int v = blockIdx.y + a.e_first;
+  const int in1 = v == 4 ? 11 : v == 5 ? 12 : v == 6 ? 10 : v == 7 ? 13 : 2 * v;
+  const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
+  constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
+  const RkCtx<T, T> rkf = rk_ctx<T>(a, kk.pc, kk.K);
+  const float ccf = a.st->f_cc[a.stage], ddcf = a.st->f_ddc[a.stage], itf = a.st->f_inv_tau;
+  const float tsf = a.st->f_ts[a.stage];
+  const bool need_k2 = (v >= 1 && v <= 3 && a.P.visc) || (v >= 4 && v <= 6 && a.P.resis);
+  const C* W = b.W2 + in1 * g.fsc;
+  CS* U = b.U + v * g.fsc;
+  C* R = b.R + v * g.fsc;
+  const unsigned tot = dkx.d * (unsigned)g.nky();  // < 2^31 for nz = 1
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
+    const unsigned r = dkx.div(i);
+    const int kx = (int)(i - r * dkx.d);
+    const int ky = g.ky_of((int)r);
+    const long long idx = (long long)ky * g.kxp + kx;
+    const cx<T> f = Store<T>::ldg(W + idx);
+    const cx<TS> u = Store<TS>::ldc(U + idx);
+    if constexpr (F32INC) {
+      const cx<float> r = a.stage > 0 ? Store<T>::ldc(R + idx) : cx_zero<float>();
+      const float k2f = need_k2 ? Cvt<float, T>::r(rkf.k2(kx, ky, 0)) : 0.0f;
+      rk.update_f32(v, f, u, r, U + idx, R + idx, k2f, kx, ky, 0, kk.pc, ccf, ddcf, itf, tsf);
+    } else {
+      const cx<TS> r = rk.r_of(R + idx);
+      TS k2 = need_k2 ? rk.k2(kx, ky, 0) : kk.ps.zero;
+      rk.update(v, cvtc<TS>(f), u, r, U + idx, R + idx, k2, kx, ky, 0);
+    }
+  }
+}
+
 // Continuity update when the mass flux is the momentum (PassArgs::mass_from_state):
 // fnl(rho) = -i k . (rho u)^ read from the state (mhdrhs.f90:206-209), then the tail and the
 // time advance of rho for every kept element.  Launched before pass E updates the momentum.
-template <class T, class TS>
-__global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk) {
+template <class T, class TS, class IDX>
+__global__ void __launch_bounds__(256) k_mass_rk(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, FastDiv dkx, FastDiv dky) {
   if (a.st->halt) return;
   using CS = typename Store<TS>::C;
   const Geo& g = a.g;
   const RkCtx<TS, T> rk = rk_ctx<T>(a, kk.ps, kk.KS);
   constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
-  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
-  const float tsf = (float)a.st->ts[a.stage], rrf = (float)a.st->r_ratio;
-  const long long nkx = g.kx_keep, nky = g.nky();
-  const long long tot = nkx * nky * g.nkz();
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
-    const int kx = (int)(i % nkx);
-    const long long r = i / nkx;
-    const int ky = g.ky_of((int)(r % nky)), kz = g.kz_of((int)(r / nky));
+  const float ccf = a.st->f_cc[a.stage], ddcf = a.st->f_ddc[a.stage], itf = a.st->f_inv_tau;
+  const float tsf = a.st->f_ts[a.stage], rrf = a.st->f_r_ratio;
+  // flat index over the kept elements: 32-bit, split by FastDiv, whenever the count allows
+  // (IDX unsigned), else 64-bit division
+  const IDX nkx = (IDX)g.kx_keep, nky = (IDX)g.nky();
+  const IDX tot = nkx * nky * (IDX)g.nkz();
+  for (IDX i = blockIdx.x * (IDX)blockDim.x + threadIdx.x; i < tot; i += (IDX)gridDim.x * blockDim.x) {
+    int kx, ky, kz;
+    if constexpr (std::is_same<IDX, unsigned>::value) {
+      const unsigned r = dkx.div(i), q = dky.div(r);
+      kx = (int)(i - r * dkx.d);
+      ky = g.ky_of((int)(r - q * dky.d));
+      kz = g.kz_of((int)q);
+    } else {
+      kx = (int)(i % nkx);
+      const IDX r = i / nkx;
+      ky = g.ky_of((int)(r % nky));
+      kz = g.kz_of((int)(r / nky));
+    }
     const long long idx = ((long long)kz * g.ny + ky) * g.kxp + kx;
     const cx<TS> m1 = Store<TS>::ldc(b.U + 1 * g.fsc + idx), m2 = Store<TS>::ldc(b.U + 2 * g.fsc + idx),
                  m3 = Store<TS>::ldc(b.U + 3 * g.fsc + idx);
@@ -1377,8 +1449,8 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS) k_passE3i(Bufs<T, TS> b, 
   // FP32 transforms with a wider state: FP32 increments and k^2 (RkCtx::update_f32)
   constexpr bool F32INC = std::is_same<T, float>::value && !std::is_same<TS, float>::value;
   const RkCtx<T, T> rkf = rk_ctx<T>(a, kk.pc, kk.K);
-  const float ccf = (float)a.st->cc[a.stage], ddcf = (float)a.st->ddc[a.stage], itf = (float)a.st->inv_tau;
-  const float tsf = (float)a.st->ts[a.stage];
+  const float ccf = a.st->f_cc[a.stage], ddcf = a.st->f_ddc[a.stage], itf = a.st->f_inv_tau;
+  const float tsf = a.st->f_ts[a.stage];
 #pragma unroll 1
   for (int m = 0; m < CL::EPT; m++) {
     int kz = x.j(m);
