@@ -80,7 +80,7 @@ LAPS_COL_PASS(launch_passA, k_passA, nky)
     using CL = Col<T, NN>;                                                                                              \
     /* 2-D: one buffer per tile (the state is read by the threads) - tiles are laid out with */                      \
     /* two buffers each, so only a single-tile block may drop the second; 3-D: the two inputs  */                      \
-    const int smB = (a.P.two_d && CL::NTILE == 1) ? CL::SMEM : 2 * CL::SMEM;                                            \
+    const int smB = ((a.P.two_d || PassBOneBuf<T, NN>::V) && CL::NTILE == 1) ? CL::SMEM : 2 * CL::SMEM;                 \
     if (!a.P.two_d && col_one_buffer<T, NN>()) throw Error{LAPS_EINVAL, "column tiles exceed shared memory"};             \
     dim3 grid((a.g.kx_keep + TX - 1) / TX, (a.g.nz + CL::NTILE - 1) / CL::NTILE,                                        \
               a.P.variant == LAPS_VARIANT_3DI ? 19 : (a.hall ? 11 : 8));                                                \

@@ -139,6 +139,13 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS)
 //   incompressible:   0..6 state; J: 7, 8, 9; grad(rho u): 10 + 3c + d = d/dx_d (rho u)_c
 // Tile: kx0..kx0+7, one z plane; reads kept ky rows, writes all y of W2.
 enum { BF_ONE = 1, BF_AX = 2, BF_MAX = -2, BF_AY = 3, BF_MAY = -3 };
+// one tile buffer per block in 3-D pass B: FP32 lines in single-tile blocks
+#ifndef LAPS_PASSB_ONEBUF
+#define LAPS_PASSB_ONEBUF 1
+#endif
+template <class T, int N> struct PassBOneBuf {
+  static constexpr bool V = LAPS_PASSB_ONEBUF && sizeof(typename Store<T>::C) == 8 && Col<T, N>::NTILE == 1;
+};
 struct BTab { signed char in0, f0, in1, f1; };
 __constant__ BTab c_btab[3][19] = {
     {{0, 1, -1, 0}, {1, 1, -1, 0}, {2, 1, -1, 0}, {3, 1, -1, 0}, {4, 1, -1, 0}, {5, 1, -1, 0}, {6, 1, -1, 0}, {7, 1, -1, 0},
@@ -191,24 +198,61 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS)
     TileLoad tl;
     tl.init(tbar);
     const int nin = e.in1 >= 0 ? 2 : 1;
-    if (threadIdx.x == 0) {
-      // only the kept ky rows of each column (the map's box is kc.box rows high)
+    // FP32 single-tile blocks hold one buffer: a second input comes into it once the threads
+    // have taken the first into registers (twice the resident blocks of two buffers)
+    constexpr bool SEQ = PassBOneBuf<T, NY>::V;
+    // only the kept ky rows of each column (the map's box is kc.box rows high); input k into
+    // buffer `buf` of every tile, announced on barrier k
+    auto issue = [&](int k, int buf) {
+      if (threadIdx.x != 0) return;
       constexpr int EW = (int)(sizeof(C) / 8);
       const KeptCopies kc(g.ky_lo, g.ky_hi, NY, tile_gran((int)sizeof(C)));
       const int nc = kc.count(NY);
       const int z0 = blockIdx.y * CL::NTILE;
       const int nt = g.nz - z0 < CL::NTILE ? g.nz - z0 : CL::NTILE;
-      for (int k = 0; k < nin; k++) {
-        tl.expect(k, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(C)));
-        for (int t = 0; t < nt; t++) {
-          C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + k) * NY * TX;  // tile t, buffer k
-          for (int i = 0; i < nc; i++) {
-            const int y0 = kc.start(i, NY);
-            tl.copy(k, dst + y0 * TX, &tmap, blockIdx.x * TX * EW, y0, (k == 0 ? e.in0 : e.in1) * g.nz + z0 + t);
+      tl.expect(k, (uint32_t)(nt * nc * kc.box * TX * (int)sizeof(C)));
+      for (int t = 0; t < nt; t++) {
+        C* dst = reinterpret_cast<C*>(smem_tma) + (t * 2 + buf) * NY * TX;  // tile t, buffer buf
+        for (int i = 0; i < nc; i++) {
+          const int y0 = kc.start(i, NY);
+          tl.copy(k, dst + y0 * TX, &tmap, blockIdx.x * TX * EW, y0, (k == 0 ? e.in0 : e.in1) * g.nz + z0 + t);
+        }
+      }
+    };
+    if constexpr (SEQ) {
+      issue(0, 0);
+      if (!tl.wait(0, a.st)) return;
+      cx<T> v[CL::EPT];
+#pragma unroll
+      for (int m = 0; m < CL::EPT; m++) {
+        const int ky = x.j(m);
+        v[m] = cx_zero<T>();
+        if (ok && g.ky_in(ky)) {
+          T ax = pc.zero, ay = pc.zero, az;
+          if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+          v[m] = bterm(Store<T>::ldc(x.at(0, m)), e.f0, ax, ay);
+        }
+      }
+      if (nin > 1) {
+        __syncthreads();  // every thread has read the first input
+        if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(1, 0);
+        if (!tl.wait(1, a.st)) return;
+#pragma unroll
+        for (int m = 0; m < CL::EPT; m++) {
+          const int ky = x.j(m);
+          if (ok && g.ky_in(ky)) {
+            T ax = pc.zero, ay = pc.zero, az;
+            if (kf) kfac(K, a.P, pc, rr, kx, ky, 0, ax, ay, az);
+            v[m] = v[m] + bterm(Store<T>::ldc(x.at(0, m)), e.f1, ax, ay);
           }
         }
       }
-    }
+#pragma unroll
+      for (int m = 0; m < CL::EPT; m++) Store<T>::stc(x.at(0, m), v[m]);
+    } else {
+    issue(0, 0);
+    if (nin > 1) issue(1, 1);
     if (!tl.wait(0, a.st) || (nin > 1 && !tl.wait(1, a.st))) return;
 #pragma unroll
     for (int m = 0; m < CL::EPT; m++) {
@@ -221,6 +265,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS)
         if (nin > 1) v = v + bterm(Store<T>::ldc(x.at(1, m)), e.f1, ax, ay);
       }
       Store<T>::stc(x.at(0, m), v);
+    }
     }
   } else {
     // 2-D: the state itself (the state type) through the threads
