@@ -184,6 +184,19 @@ def pass_bytes(n, kx_keep, nky, nkz, hall=True, aeb=True, eS=16, eT=16, mass=Tru
     return {"A_inv_z": A, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
 
 
+# the same for one 2-D compressible member (nz = 1: no pass A; pass B reads the 8 state fields
+# itself and writes 11 (state + current); pass E is elementwise over the kept (kx, ky) modes,
+# the continuity update included); Hall on, expanding box off, continuity from the momentum
+def pass_bytes_2d(n, kx_keep, nky, eS=16, eT=16):
+    kxp8 = int(math.ceil(kx_keep / 8.0) * 8)
+    na, nfl, nd = 11, 12, 13
+    B = kxp8 * (8 * nky * eS + na * n * eT)
+    C = n * kx_keep * (na + nfl) * eT
+    D = kxp8 * (nfl * n * eT + nd * nky * eT)
+    E = kxp8 * nky * (nd * eT + 8 * 2 * (eS + eT))
+    return {"A_inv_z": 0, "B_inv_y": B, "C_x_flux": C, "D_fwd_y": D, "E_fwd_z_rk": E}
+
+
 # the same for the incompressible step: A reads 7 state fields and writes 12 (u, B, J, grad
 # terms), B 12 -> 19, C 19 -> 6 (pressure flux, E), D 6 -> 8, E reads 8 and updates 8 state
 # fields (U and R read and written on kept kz)
@@ -647,6 +660,17 @@ def run_ensemble(args):
         cpu = {"value": pts / cpu_s, "unit": "grid-point-steps/s", "cores": laps3d._WORKERS, "kind": "port",
                "sample": f"one member of each grid size {sorted(seen)}, 1 warm-up + 2 timed steps each "
                          f"(numpy + scipy.fft 2-D restatement)"}
+    # whole-step roofline: the algorithmic bytes of every member's three stages (pass_bytes_2d)
+    # over the timed step, against the measured copy bandwidth; kernel launches from each
+    # member's own count per step
+    eS, eT = PRECISIONS[args.precision][2:4]
+    step_bytes, launches = 0, 0
+    for m in b.members:
+        inf = m.info()
+        step_bytes += 3 * sum(pass_bytes_2d(m.p.nx, inf.kx_keep, inf.ky_keep, eS=eS, eT=eT).values())
+        launches += inf.kernels_per_step
+    peak, src = peaks()
+    achieved = step_bytes / (el / args.steps) / 1e9
     line = {
         "metric": "grid-point-steps/s of a 64-member 2-D Hall-MHD ensemble", "value": value, "unit": "grid-point-steps/s",
         "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": el / args.steps * 1e3,
@@ -659,7 +683,10 @@ def run_ensemble(args):
         "status_nonzero_members": int((st != 0).sum()),
         "schedules": schedules,
         "cpu_baseline": cpu,
-        "gpu_launches": None,
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "whole step (every pass of every member)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src, "traffic": None,
+                     "algorithmic_bytes_per_step": step_bytes},
         "e2e": {"value": npts * args.steps / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
