@@ -664,6 +664,12 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int OCC = OCC2 < 1 ? 1 : OCC2;
 };
 
+#ifndef LAPS_DD_SHARED_FFT
+#define LAPS_DD_SHARED_FFT 1
+#endif
+#ifndef LAPS_PAIR_POINTS
+#define LAPS_PAIR_POINTS 1
+#endif
 template <class T, class TS, int NX, int CFL, int INCOMP>
 __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)>::THREADS,
                                   PassCCfg<NX, (int)sizeof(typename Store<T>::C)>::OCC) k_passC(Bufs<T, TS> b, PassArgs a, PassK<T, TS> kk, const typename Store<T>::C* __restrict__ twx) {
@@ -694,7 +700,7 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   // float-float 256-point rows: one (called) copy of the transform for both directions (pass
   // time -9 %: the kernel stalled on instruction fetch; FP64 rows, ALU-bound, lose 3 % and
   // keep both inlined copies)
-  constexpr bool SHARED_FFT = std::is_same<T, dd>::value && NX == 256 && CF::PAIRED;
+  constexpr bool SHARED_FFT = LAPS_DD_SHARED_FFT && std::is_same<T, dd>::value && NX == 256 && CF::PAIRED;
   if constexpr (CF::PAIRED) {
     // ---- inverse x-transform of row pairs: Z = X_a + i X_b over the full line (the
     // imaginary parts of the DC and Nyquist terms are dropped, as the reference's c2r does)
@@ -854,10 +860,37 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
     return;
   }
   // ---- physics per point, in place (inputs and outputs of a point share its slots)
-  const T inv_tau = Real<T>::from_d(a.st->inv_tau);
-  T inv_rho0;
-  if constexpr (std::is_same<T, float>::value) inv_rho0 = a.st->f_inv_rho0;
-  else inv_rho0 = Real<T>::from_d(a.st->inv_rho0);
+  T inv_tau, inv_rho0;
+  if constexpr (std::is_same<T, float>::value) {
+    inv_tau = a.st->f_inv_tau;
+    inv_rho0 = a.st->f_inv_rho0;
+  } else {
+    inv_tau = Real<T>::from_d(a.st->inv_tau);
+    inv_rho0 = Real<T>::from_d(a.st->inv_rho0);
+  }
+  if constexpr (LAPS_PAIR_POINTS && std::is_same<T, float>::value && CF::PAIRED) {
+    // FP32 paired rows: the two rows of a pair share each complex slot (row 2p in .x, row
+    // 2p+1 in .y), so one thread takes both points at an x, with one 8-byte load and one
+    // 8-byte store per field (a warp then reads consecutive 8-byte slots: no bank conflict);
+    // the first point's outputs wait in registers until the second point produces its own
+    constexpr int NPAIR = CF::ROWS / 2;
+    C* sc2 = reinterpret_cast<C*>(smem_raw);
+#pragma unroll 1
+    for (int p = threadIdx.x; p < NPAIR * NX; p += CF::THREADS) {
+      const int pr = p / NX, xx = p - pr * NX;
+      C* base = sc2 + pr * CF::NF * CF::LCP + sm_idx<1>(xx);
+      T q0[NQ], q1[NQ];
+#pragma unroll
+      for (int f = 0; f < NQ; f++) {
+        const C v = f < nin ? base[f * CF::LCP] : C{0.f, 0.f};
+        q0[f] = v.x;
+        q1[f] = v.y;
+      }
+      T o0[19];
+      PH::eval(q0, [&](int k, T v) { o0[k] = v; }, pc, a.P, inv_tau, inv_rho0);
+      PH::eval(q1, [&](int k, T v) { if ((c_fused >> k) & 1) base[k * CF::LCP] = C{o0[k], v}; }, pc, a.P, inv_tau, inv_rho0);
+    }
+  } else
 #pragma unroll 1
   for (int p = threadIdx.x; p < CF::ROWS * NX; p += CF::THREADS) {
     SR* base = point_base(p);
@@ -1096,6 +1129,9 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOccN<T, NY>::V)
 }
 
 // ============================================================================ pass E
+#ifndef LAPS_E_CHUNK
+#define LAPS_E_CHUNK 4  // elements whose state and RK-register loads pass E issues together
+#endif
 // Per-element tail of the spectral right-hand side and the time advance of variable v:
 // expansion damping (mhdrhs.f90:235-251), explicit diffusion (:253-275), the RK3 update with
 // implicit diffusion (rktmod.f90:34-62) and the dealias mask or filter (dealiasing.f90:70-113).
@@ -1318,7 +1354,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
   C* R = b.R + v * g.fsc + col;
   // elements in chunks of CH: the state and RK-register loads of a chunk are issued together
   // ahead of its arithmetic (the update's stores may alias them as far as the compiler knows)
-  constexpr int CH = CL::EPT < 4 ? CL::EPT : 4;
+  constexpr int CH = CL::EPT < LAPS_E_CHUNK ? CL::EPT : LAPS_E_CHUNK;
   // the RK register as the update reads it: FP32 as stored for FP32 increments, else in TS
   using RV = typename std::conditional<F32INC, float, TS>::type;
 #pragma unroll 1
