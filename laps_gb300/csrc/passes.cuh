@@ -882,13 +882,13 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
       T q0[NQ], q1[NQ];
 #pragma unroll
       for (int f = 0; f < NQ; f++) {
-        const C v = f < nin ? base[f * CF::LCP] : C{0.f, 0.f};
-        q0[f] = v.x;
-        q1[f] = v.y;
+        const cx<T> v = f < nin ? Store<T>::ldc(base + f * CF::LCP) : cx_zero<T>();
+        q0[f] = v.re;
+        q1[f] = v.im;
       }
       T o0[19];
       PH::eval(q0, [&](int k, T v) { o0[k] = v; }, pc, a.P, inv_tau, inv_rho0);
-      PH::eval(q1, [&](int k, T v) { if ((c_fused >> k) & 1) base[k * CF::LCP] = C{o0[k], v}; }, pc, a.P, inv_tau, inv_rho0);
+      PH::eval(q1, [&](int k, T v) { if ((c_fused >> k) & 1) Store<T>::stc(base + k * CF::LCP, cx<T>{o0[k], v}); }, pc, a.P, inv_tau, inv_rho0);
     }
   } else
 #pragma unroll 1
