@@ -67,6 +67,14 @@ __device__ __forceinline__ dd operator/(dd a, dd b) {
   dd q = dd_fast_two_sum(q1, q2);
   return q + dd{q3, 0.f};
 }
+// 1 / b: the nearest float r0 of 1 / b.hi, then one Newton step r0 + r0 (1 - b r0) with the
+// residual 1 - b r0 formed in float-float (its error is of order (1 - b r0)^2 ~ 2^-48, the
+// float-float precision); a quarter of the instructions of operator/ with three quotient terms
+__device__ __forceinline__ dd dd_recip(dd b) {
+  const float r0 = __frcp_rn(b.hi);
+  const dd e = dd{1.f, 0.f} - dd_mul_f(b, r0);
+  return dd_fast_two_sum(r0, __fmul_rn(r0, e.hi));
+}
 __device__ __forceinline__ dd dd_sqrt(dd a) {
   if (!(a.hi > 0.f)) return {sqrtf(a.hi), 0.f};  // 0, negative (NaN) or NaN propagate
   float s = __fsqrt_rn(a.hi);
@@ -91,6 +99,11 @@ __host__ __device__ __forceinline__ dd dd_from_double(double d) {
 __host__ __device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
 
 // ------------------------------------------------------------------------------ traits
+// LAPS_DD_RECIP: float-float reciprocals by dd_recip (1 / rho of the fluxes, the implicit
+// diffusion factor); 0 restores the float-float division
+#ifndef LAPS_DD_RECIP
+#define LAPS_DD_RECIP 1
+#endif
 // Real<T>: scalar ops used by generic code.  `cst(x)` turns a compile-time double into T.
 template <class T> struct Real;
 template <> struct Real<double> {
@@ -109,6 +122,7 @@ template <> struct Real<double> {
   __device__ __forceinline__ static bool isnan_(double x) { return x != x; }
   __device__ __forceinline__ static double min_(double a, double b) { return b < a ? b : a; }
   __device__ __forceinline__ static double inf() { return __longlong_as_double(0x7FF0000000000000ll); }
+  __device__ __forceinline__ static double recip(double x) { return 1.0 / x; }
 };
 template <> struct Real<dd> {
   __device__ __forceinline__ static dd cst(double x) { return dd_from_double(x); }
@@ -122,6 +136,7 @@ template <> struct Real<dd> {
   __device__ __forceinline__ static bool isnan_(dd x) { return x.hi != x.hi; }
   __device__ __forceinline__ static dd min_(dd a, dd b) { return b < a ? b : a; }
   __device__ __forceinline__ static dd inf() { return {__int_as_float(0x7f800000), 0.f}; }
+  __device__ __forceinline__ static dd recip(dd x) { return LAPS_DD_RECIP ? dd_recip(x) : dd{1.f, 0.f} / x; }
 };
 template <> struct Real<float> {
   __device__ __forceinline__ static float cst(double x) { return (float)x; }
@@ -136,6 +151,7 @@ template <> struct Real<float> {
   __device__ __forceinline__ static bool isnan_(float x) { return x != x; }
   __device__ __forceinline__ static float min_(float a, float b) { return b < a ? b : a; }
   __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
+  __device__ __forceinline__ static float recip(float x) { return 1.0f / x; }
 };
 
 // Division and square root policies of the CFL bound: exact in the arithmetic type, or the

@@ -408,7 +408,7 @@ struct Flux {
   __device__ __forceinline__ static void eval(const T* q, OUT out, const PT<T>& c, const Phys& P, T inv_tau, T inv_rho0) {
     const T half = c.half, gm1 = c.gm1;
     const T rho = q[0], mx = q[1], my = q[2], mz = q[3], Bx = q[4], By = q[5], Bz = q[6], e = q[7];
-    const T rinv = c.one / rho;
+    const T rinv = Real<T>::recip(rho);
     const T ux = mx * rinv, uy = my * rinv, uz = mz * rinv;
     const T b2 = Bx * Bx + By * By + Bz * Bz;
     const T p = (e - half * (mx * ux + my * uy + mz * uz + b2)) * gm1;
@@ -553,7 +553,7 @@ struct FluxI {
     out(0, -mx * g[0] - my * g[1] - mz * g[2] + Jy * Bz - Jz * By);
     out(1, -mx * g[3] - my * g[4] - mz * g[5] + Jz * Bx - Jx * Bz);
     out(2, -mx * g[6] - my * g[7] - mz * g[8] + Jx * By - Jy * Bx);
-    const T rinv = c.one / rho;
+    const T rinv = Real<T>::recip(rho);
     const T ux = mx * rinv, uy = my * rinv, uz = mz * rinv;
     T ex = uz * By - uy * Bz, ey = ux * Bz - uz * Bx, ez = uy * Bx - ux * By;
     if (P.hall) {
@@ -1138,6 +1138,18 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOccN<T, NY>::V)
 // T: the state type (the update's arithmetic); TR: the type of the RK register, which holds
 // the previous stages' right-hand side (the transforms' type: FP32 in the FP32-transform
 // modes, where the right-hand side carries FP32 accuracy anyway)
+// u / d of the implicit diffusion step: a float-float state takes one reciprocal and two
+// products instead of two float-float divisions (roundings of ~2^-48, far inside the mode's
+// 1e-12 bound; LAPS_DD_RECIP=0 restores the divisions); FP64 divides as the reference
+template <class T> __device__ __forceinline__ cx<T> implicit_div(cx<T> u, T d) {
+  if constexpr (LAPS_DD_RECIP && std::is_same<T, dd>::value) {
+    const T r = Real<T>::recip(d);
+    return {u.re * r, u.im * r};
+  } else {
+    return {u.re / d, u.im / d};
+  }
+}
+
 template <class T, class TR = T>
 struct RkCtx {
   using CR = typename Store<TR>::C;
@@ -1176,11 +1188,11 @@ struct RkCtx {
     if (store_rk) Store<TR>::stc(R, cvtc<TR>(fnl));
     if (mom && P->visc && !P->visc_exp) {
       T d = ts * k2 * pc->nu + pc->one;
-      un = {un.re / d, un.im / d};
+      un = implicit_div(un, d);
     }
     if (mag && P->resis && !P->resis_exp) {
       T d = ts * k2 * pc->eta + pc->one;
-      un = {un.re / d, un.im / d};
+      un = implicit_div(un, d);
     }
     if (P->dealias == 1 || P->dealias == 3) {
       if (kx >= K->kxlim[kz * g->ny + ky]) un = cx_zero<T>();
