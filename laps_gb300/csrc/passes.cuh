@@ -933,11 +933,17 @@ __global__ void __launch_bounds__(PassCCfg<NX, (int)sizeof(typename Store<T>::C)
   if (CFL && cand_late) eval_list();  // after this warp's share of the transforms
 }
 
-// Resident blocks per SM the register budget of passes D and E is set for (FP32 lines): 5
-// measured best at 256^3 (1, no bound: +3 % step time; 6 and 7 spill: +9 %, +11 %);
-// LAPS_MINB_COL overrides it at build time for tuning sweeps.
+// Resident blocks per SM the register budget of passes D and E is set for (FP32 lines) and
+// how they transform their two input tiles: one after the other with 6 blocks (the shared-
+// memory limit of two 16 KB tiles) measured best at 256^3 (passes D + E -0.06 ms per step).
+// Transforming both tiles together (LAPS_COL_PAIR_FFT=1: fft_lines_pair, half the barriers
+// but twice the live elements per thread) needs 96 registers and runs 5 blocks; the pairs
+// with 6 or 7 blocks spilled (+9 %, +11 %).  Both macros override the choice at build time.
 #ifndef LAPS_MINB_COL
-#define LAPS_MINB_COL 5
+#define LAPS_MINB_COL 6
+#endif
+#ifndef LAPS_COL_PAIR_FFT
+#define LAPS_COL_PAIR_FFT 0
 #endif
 // (float-float: 4 and FP64: 3, the budgets the compiler picks for them without a bound)
 template <class T> struct ColOcc {
@@ -1019,7 +1025,7 @@ __global__ void __launch_bounds__(Col<T, NY>::THREADS, ColOccN<T, NY>::V)
       }
     }
   };
-  constexpr bool PAIR = sizeof(C) == 8;
+  constexpr bool PAIR = sizeof(C) == 8 && LAPS_COL_PAIR_FFT;
   // one shared-memory tile (1024-point columns of 16-byte elements): the inputs come one
   // after the other into buffer 0, and the tile a later input would have found in the other
   // buffer is kept as each thread's own elements in registers (rb)
@@ -1346,7 +1352,7 @@ __global__ void __launch_bounds__(Col<T, NZ>::THREADS, ColOccN<T, NZ>::V)
     }
     __syncthreads();
   }
-  if constexpr (sizeof(C) == 8) {  // FP32 lines: the two inputs transformed together
+  if constexpr (sizeof(C) == 8 && LAPS_COL_PAIR_FFT) {  // FP32 lines: the two inputs transformed together
     fft_lines_pair<T, NZ, -1, TX, 1>(x.buf(0), x.buf(1), nin > 1, x.c, x.t, twz, 1);
   } else {
     fft_lines<T, NZ, -1, TX, 1>(x.buf(0), x.c, x.t, true, twz, 1);
