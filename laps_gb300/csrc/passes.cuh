@@ -635,6 +635,11 @@ constexpr unsigned c_fused = 0x7FFFFu & ~((1u << 6) | (1u << 9) | (1u << 10));
 #ifndef LAPS_PASSC_PAIR_1024
 #define LAPS_PASSC_PAIR_1024 0
 #endif
+// resident blocks of FP32 pass C the register budget is set for: 5 (64 registers, 30 warps per
+// SM) measured 2 % faster at 256^3 than 4 (80 registers); the build-time override is for sweeps
+#ifndef LAPS_PASSC_OCC_F32
+#define LAPS_PASSC_OCC_F32 5
+#endif
 template <int NX, int CB> struct PassCCfg {
   static constexpr int H = NX / 2;
   static constexpr int TPL = Plan<H>::TPL;
@@ -658,7 +663,7 @@ template <int NX, int CB> struct PassCCfg {
   static constexpr int SMEM = (PAIRED ? (ROWS / 2) * NF * LCP : ROWS * NF * LC) * CB;  // CB: bytes of one complex
   // resident blocks per SM the register budget is set for: at most 4 (FP32 lines) or 2,
   // within the shared memory and the 2048 threads of an SM
-  static constexpr int OCC0 = CB == 8 ? 4 : 2;
+  static constexpr int OCC0 = CB == 8 ? LAPS_PASSC_OCC_F32 : 2;
   static constexpr int OCC1 = (227 * 1024) / (SMEM + 1024) < OCC0 ? (227 * 1024) / (SMEM + 1024) : OCC0;
   static constexpr int OCC2 = 2048 / THREADS < OCC1 ? 2048 / THREADS : OCC1;
   static constexpr int OCC = OCC2 < 1 ? 1 : OCC2;
