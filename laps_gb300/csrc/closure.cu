@@ -41,7 +41,10 @@
 namespace laps {
 
 constexpr int CONV_TILE = 128;     // voxels per tile (MMA M)
-constexpr int CONV_STAGES = 6;     // activation stages in flight
+#ifndef LAPS_CONV_STAGES
+#define LAPS_CONV_STAGES 6
+#endif
+constexpr int CONV_STAGES = LAPS_CONV_STAGES;  // activation stages in flight
 constexpr int CONV_THREADS = 192;  // producer warp, MMA warp, 4 epilogue warps
 #ifndef LAPS_WGRAD_SWAP
 #define LAPS_WGRAD_SWAP false
@@ -727,10 +730,15 @@ static void launch_conv3(cudaStream_t s, const void* x, const void* wpk, ConvArg
   LAPS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
   LAPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CONV_THREADS, CF::SMEM));
-  int dev = 0, nsm = 0;
+  int dev = 0, nsm = 0, smem_sm = 0;
   LAPS_CK(cudaGetDevice(&dev));
   LAPS_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  LAPS_CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   if (per_sm < 1) throw Error{LAPS_ECUDA, "conv kernel does not fit on an SM"};
+  // the occupancy query answers for the default shared-memory carveout; with the full
+  // carveout two blocks fit (128 registers x 192 threads, ~111 KB each): take the larger
+  // count (blocks are independent, so blocks that do not fit at once only start later)
+  if (per_sm < 2 && 2 * (CF::SMEM + 2048) <= smem_sm) per_sm = 2;
   const int grid = a.ntiles < nsm * per_sm ? a.ntiles : nsm * per_sm;
   const CUtensorMap tm = conv_tensor_map_box(x, (long long)a.nz * a.ny * (a.nx + 2), KC * 8, CF::A_ROWS);
   kern<<<grid, CONV_THREADS, CF::SMEM, s>>>(tm, reinterpret_cast<const uint4*>(wpk), a);
