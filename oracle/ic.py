@@ -1,6 +1,6 @@
 """CPU restatement of the reference's fresh-start initial conditions (test infrastructure).
 
-This module is the checker for ``laps_init_fields``: the parity tests compare the device's
+This module is the oracle of ``laps_init_fields``: the parity tests compare the device's
 generated state with the arrays built here.  Nothing in the product imports it.
 
 It follows, point by point and mode by mode in float64 numpy:

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the shipped GPU path imports this module; it is
 imported only by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py``, always as the checker, never as the thing measured or shipped.
+``bench.py``, always as the oracle, never as the thing measured or shipped.
 
 PARITY UNPINNED.  The reference (Fortran 90 + MPI + FFTW3, ``src_compressible/``) cannot
 be compiled here (no Fortran compiler, no MPI, no FFTW) and ships no tests, golden vectors

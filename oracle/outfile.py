@@ -1,4 +1,4 @@
-"""The reference's output / restart file, restated in numpy (test infrastructure: the checker
+"""The reference's output / restart file, restated in numpy (test infrastructure: the oracle
 of laps_write_output / laps_read_restart).
 
 ``outNNN.dat`` (``src_compressible/mhdoutput.f90:72-131``, ``restart.f90:17-63``; the 2-D and

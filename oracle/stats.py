@@ -1,6 +1,6 @@
 """CPU restatement of the reference's angle statistics (test infrastructure).
 
-The checker for ``laps_angle_statistics``: the perpendicular angles between the increments
+The oracle of ``laps_angle_statistics``: the perpendicular angles between the increments
 of u and b = B / sqrt(<rho>), and of z+ = u - b and z- = u + b, at lags 1 .. n/2 along one
 axis, following theta_ub_zpm_perp_only (data_process/3D_C/statistics.c:10-356) with numpy
 arrays in place of its point loop: means (:86-101), increments with periodic wrap
