@@ -98,6 +98,33 @@ def test_alfven_wave_known_answer():
     assert np.abs(o.uu[5] + 0.1 * np.cos(x - o.time) * dec).max() < 1e-5
 
 
+def test_force_free_field_decays_by_the_implicit_factor():
+    """A Beltrami field B = (sin z, cos z, 0) with u = 0 is force-free (J = B) and keeps a
+    uniform total pressure, so only resistivity acts: every RK stage divides the k = 1 modes by
+    1 + ts_i eta k^2 with ts = (8/15, 2/15, 1/3) dt (rktmod.f90:34-62, implicit branch), and the
+    field after the steps is the initial one times the product of those factors, to round-off.
+    The flow stays at rest."""
+    n, eta = 16, 0.05
+    z = np.arange(n) * (2 * math.pi / n)
+    prim = np.zeros((8, n, n, n))
+    prim[0] = 1.0
+    prim[4] = np.sin(z)[:, None, None]
+    prim[5] = np.cos(z)[:, None, None]
+    prim[7] = 0.5
+    kw = dict(if_resis=1, resistivity=eta, dealias_option=1, cfl=0.3)
+    o = laps3d.restart(n, kw, prim)
+    amp = 1.0
+    for _ in range(10):
+        o.vardt()
+        for ts in (8.0 / 15.0, 2.0 / 15.0, 1.0 / 3.0):
+            amp /= 1.0 + ts * o.dt * eta
+        o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    assert amp < 0.99
+    assert np.abs(o.uu[4] - amp * prim[4]).max() < 1e-13
+    assert np.abs(o.uu[5] - amp * prim[5]).max() < 1e-13
+    assert np.abs(o.uu[1:4]).max() < 1e-13
+
+
 def test_conservation_ideal():
     """Mean density, momentum, field and total energy are invariants of the ideal equations."""
     prim = turbulence_ic(16, seed=4, rms_u=0.3, rms_b=0.3, kmax=3)
