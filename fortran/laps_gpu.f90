@@ -54,6 +54,13 @@ module laps_gpu
         real(c_double) :: max_divB, max_divB_real, max_divV_real, e_kin, e_mag, h_cross, h_mag
     end type laps_diag
 
+    type, bind(C) :: laps_info
+        integer(c_long_long) :: device_bytes
+        integer(c_int) :: kx_keep, ky_keep, kz_keep
+        integer(c_int) :: kernels_per_step
+        integer(c_int) :: graph
+    end type laps_info
+
     interface
         integer(c_int) function laps_params_default(p) bind(C, name='laps_params_default')
             import :: c_int, laps_params
@@ -188,6 +195,88 @@ module laps_gpu
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx
             integer(c_int), value :: timeout_ms
+        end function
+        ! the granular calls of the reference's stage, in its order (mhd.f90:303-325)
+        integer(c_int) function laps_transform_uu_k2r(ctx, uu) bind(C, name='laps_transform_uu_k2r')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: uu(*)
+        end function
+        integer(c_int) function laps_update_prim(ctx, uu_prim) bind(C, name='laps_update_prim')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: uu_prim(*)
+        end function
+        ! uu_fourier(kx,ky,kz,1:8) as interleaved (re, im) pairs
+        integer(c_int) function laps_download_spectral(ctx, uf) bind(C, name='laps_download_spectral')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: uf(*)
+        end function
+        integer(c_int) function laps_upload_spectral(ctx, uf) bind(C, name='laps_upload_spectral')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(in) :: uf(*)
+        end function
+        integer(c_int) function laps_get_time(ctx, time, dt) bind(C, name='laps_get_time')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: time, dt
+        end function
+        integer(c_int) function laps_get_info(ctx, info) bind(C, name='laps_get_info')
+            import :: c_int, c_ptr, laps_info
+            type(c_ptr), value :: ctx
+            type(laps_info), intent(out) :: info
+        end function
+        integer(c_int) function laps_step_profiled(ctx, nsteps, pass_ms, total_ms, status) &
+                bind(C, name='laps_step_profiled')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nsteps
+            real(c_double), intent(out) :: pass_ms(6), total_ms
+            integer(c_int), intent(out) :: status
+        end function
+        ! data_process/3D_C/statistics.c on the device: out(n_axis, 4)
+        integer(c_int) function laps_angle_statistics(ctx, axis, out) bind(C, name='laps_angle_statistics')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: axis
+            real(c_double), intent(out) :: out(*)
+        end function
+        integer(c_int) function laps_set_schedule(ctx, bits) bind(C, name='laps_set_schedule')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: bits
+        end function
+        integer(c_int) function laps_get_schedule(ctx, bits) bind(C, name='laps_get_schedule')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), intent(out) :: bits
+        end function
+        integer(c_int) function laps_batch_size(batch) bind(C, name='laps_batch_size')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: batch
+        end function
+        ! device arrays (c_loc of a CUDA Fortran / OpenACC device array, or a cudaMalloc pointer)
+        integer(c_int) function laps_transform_uu_real_to_fourier_noalloc(uu, uf, nx, ny, nz, nfields, stream) &
+                bind(C, name='laps_transform_uu_real_to_fourier_noalloc')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: uu, uf
+            integer(c_int), value :: nx, ny, nz, nfields
+            type(c_ptr), value :: stream
+        end function
+        integer(c_int) function laps_state_real_device(ctx, uu_dev) bind(C, name='laps_state_real_device')
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx, uu_dev
+        end function
+        integer(c_int) function laps_add_spectral_device(ctx, duf_dev, scale) bind(C, name='laps_add_spectral_device')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx, duf_dev
+            real(c_double), value :: scale
+        end function
+        type(c_ptr) function laps_batch_last_error(batch) bind(C, name='laps_batch_last_error')
+            import :: c_ptr
+            type(c_ptr), value :: batch
         end function
         type(c_ptr) function laps_last_error(ctx) bind(C, name='laps_last_error')
             import :: c_ptr

@@ -106,7 +106,7 @@ def _fortran_type_fields(name):
 
 
 @pytest.mark.parametrize("name,cls", [("laps_params", ffi.laps_params), ("laps_ic", ffi.laps_ic),
-                                      ("laps_diag", ffi.laps_diag)])
+                                      ("laps_diag", ffi.laps_diag), ("laps_info", ffi.laps_info)])
 def test_struct_fields_agree_across_bindings(name, cls):
     """The header's struct, the ctypes mirror and the Fortran bind(C) type list the same
     fields in the same order."""
@@ -122,6 +122,10 @@ def test_fortran_module_binds_the_stepping_entry_points():
                "laps_diagnostics", "laps_calc_flux", "laps_calc_rhs", "laps_write_output", "laps_read_restart"):
         assert fn in bound, fn
     assert bound <= set(header_functions())
+    # every entry point a Fortran host can use; the closure's convolution and data-path calls
+    # take BF16 tensors of the training framework and are bound from Python only
+    torch_side = {f for f in header_functions() if f.startswith(("laps_conv3_", "laps_closure_"))}
+    assert set(header_functions()) - torch_side <= bound, sorted(set(header_functions()) - torch_side - bound)
     assert ctypes.sizeof(ffi.laps_ic) == 2 * 4 + 17 * 8 + 4 * 4 + 9 * 8
 
 
