@@ -150,3 +150,46 @@ def test_post_processing_calls_need_a_context(lib):
     ic = ffi.ic_params(ifield=3)
     assert lib.laps_init_fields(None, ctypes.byref(ic), None, 0) == ffi.LAPS_EINVAL
     assert lib.laps_angle_statistics(None, 0, None) == ffi.LAPS_EINVAL
+
+
+def _c_prototypes():
+    """name -> [(type, is_pointer)] of every function the header declares."""
+    txt = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "laps_gpu.h").read_text(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(laps_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", txt):
+        args = [a.strip() for a in m.group(2).split(",") if a.strip() and a.strip() != "void"]
+        out[m.group(1)] = [("*" in a, a) for a in args]
+    return out
+
+
+def _fortran_interfaces():
+    """name -> {argument: passed by value} of every interface body in the Fortran module."""
+    txt = (ROOT / "fortran" / "laps_gpu.f90").read_text().replace("&\n", " ")
+    out = {}
+    for m in re.finditer(r"(?:function|subroutine)\s+(\w+)\(([^)]*)\)\s*bind\(C, name='(laps_\w+)'\)(.*?)end (?:function|subroutine)",
+                         txt, flags=re.S):
+        args = [a.strip().lower() for a in m.group(2).split(",") if a.strip()]
+        by_value = {}
+        for line in m.group(4).splitlines():
+            line = line.split("!", 1)[0]
+            if "::" not in line or line.strip().lower().startswith("import"):
+                continue
+            attrs, names = line.split("::", 1)
+            for v in names.split(","):
+                by_value[re.sub(r"\(.*\)", "", v).strip().lower()] = "value" in attrs.lower()
+        out[m.group(3)] = (args, by_value)
+    return out
+
+
+def test_fortran_interfaces_match_the_c_prototypes():
+    """Every Fortran interface has the C function's argument count, passes by value exactly
+    the arguments the C prototype takes by value, and declares every argument."""
+    protos = _c_prototypes()
+    for name, (args, by_value) in _fortran_interfaces().items():
+        c = protos[name]
+        assert len(args) == len(c), name
+        for a, (is_ptr, decl) in zip(args, c):
+            assert a in by_value, (name, a)
+            # a C pointer is passed by reference, or as type(c_ptr) by value (device / opaque)
+            if not is_ptr:
+                assert by_value[a], (name, a, decl)
