@@ -125,6 +125,32 @@ def test_force_free_field_decays_by_the_implicit_factor():
     assert np.abs(o.uu[1:4]).max() < 1e-13
 
 
+def test_beltrami_flow_decays_by_the_implicit_viscous_factor():
+    """u = (sin z, cos z, 0) with B = 0 and uniform density: no advection (u . grad u = 0),
+    a uniform |u| and total energy, hence a uniform pressure, so viscosity is all that acts on
+    the momentum: each RK stage divides its k = 1 modes by 1 + ts_i nu k^2 (rktmod.f90:34-62),
+    to round-off."""
+    n, nu = 16, 0.05
+    z = np.arange(n) * (2 * math.pi / n)
+    prim = np.zeros((8, n, n, n))
+    prim[0] = 1.0
+    prim[1] = np.sin(z)[:, None, None]
+    prim[2] = np.cos(z)[:, None, None]
+    prim[7] = 0.5
+    o = laps3d.restart(n, dict(if_visc=1, viscosity=nu, dealias_option=1, cfl=0.3), prim)
+    amp = 1.0
+    for _ in range(10):
+        o.vardt()
+        for ts in (8.0 / 15.0, 2.0 / 15.0, 1.0 / 3.0):
+            amp /= 1.0 + ts * o.dt * nu
+        o.evolve(); o.time += o.dt; o.evolve_radius(o.time)
+    assert amp < 0.99
+    assert np.abs(o.uu[1] - amp * prim[1]).max() < 1e-13
+    assert np.abs(o.uu[2] - amp * prim[2]).max() < 1e-13
+    assert np.abs(o.uu[3]).max() < 1e-13 and np.abs(o.uu[4:7]).max() < 1e-13
+    assert np.abs(o.uu[0] - 1.0).max() < 1e-13
+
+
 def test_conservation_ideal():
     """Mean density, momentum, field and total energy are invariants of the ideal equations."""
     prim = turbulence_ic(16, seed=4, rms_u=0.3, rms_b=0.3, kmax=3)
